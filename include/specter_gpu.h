@@ -1,0 +1,148 @@
+/*
+ * specter_gpu.h — C ABI of the GB300 (sm_103a) implementation of SPECTER's per-RK-stage hot path.
+ *
+ * The Fortran driver reaches these entry points through iso_c_binding;
+ * each one replaces the reference routine cited beside it (paths inside specter-cfd/SPECTER).
+ *
+ * Conventions
+ *   - Every function returns an int status: 0 = SPECTER_OK, otherwise one of the codes below;
+ *     specter_last_error() returns a message for the last failure on the calling thread.
+ *     The reference's equivalent is PRINT + MPI_FINALIZE + STOP (e.g. fcgram_mod.f90:113-141).
+ *   - Fields are device-resident handles owned by the library.  Host arrays passed to
+ *     specter_field_upload/download use the reference layouts: complex C(nz, ny, nx/2+1)
+ *     (z fastest, interleaved re/im) and real R(nx, ny, nz) (x fastest), in the plan's
+ *     precision (FP64: double, FP32: float).  nz is the TOTAL z size including Cz.
+ *   - All work of a plan runs in order on the plan's CUDA stream; calls return once the work
+ *     is enqueued, except reductions (which return a host scalar) and downloads.
+ *   - The `comm` argument of the reference (MPI communicator) has no counterpart: one GPU.
+ */
+#ifndef SPECTER_GPU_H
+#define SPECTER_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    SPECTER_OK = 0,
+    SPECTER_ERR_SHAPE = 1,     /* unsupported grid shape / periodicity */
+    SPECTER_ERR_TABLE = 2,     /* FC-Gram table missing or short (fcgram_mod.f90:225-249) */
+    SPECTER_ERR_BC = 3,        /* unsupported boundary-condition combination */
+    SPECTER_ERR_OOM = 4,       /* device allocation failed */
+    SPECTER_ERR_CUDA = 5,      /* CUDA runtime error */
+    SPECTER_ERR_NONFINITE = 6, /* non-finite value detected in the state */
+    SPECTER_ERR_ARG = 7,       /* bad argument (null handle, wrong field kind, ...) */
+    SPECTER_ERR_TIMEOUT = 8,   /* a bounded device wait gave up */
+    SPECTER_ERR_STATE = 9      /* handle used with a different plan / precision */
+};
+
+enum { SPECTER_FP64 = 0, SPECTER_FP32 = 1 };            /* plan precision */
+enum { SPECTER_COMPLEX = 0, SPECTER_REAL = 1 };         /* field kind */
+enum { SPECTER_HD = 0, SPECTER_BOUSS = 1 };             /* solver (src/include/hd, bouss) */
+
+typedef struct specter_plan specter_plan;
+typedef struct specter_field specter_field;
+typedef struct specter_solver specter_solver;
+
+const char *specter_last_error(void);
+int specter_version(void);
+int specter_device_count(int *count);
+
+/* ---- plan: fcgram_create_plan (src/fftp/fcgram_mod.f90:49-144) + grid/kes setup
+ *      (src/specter.fpp:683-800).  n = (nx, ny, nz) totals, c = (Cx, Cy, Cz), o = (ox, oy, oz)
+ *      as in the reference (x, y periodic: Cx = Cy = ox = oy = 0).  len = (Lx, Ly, Lz): Lx, Ly
+ *      in units of 2*pi, Lz in units of 1 (boxparams namelist, specter.fpp:379-394).
+ *      tdir: directory holding A{C}-{d}.dat and Q{d}.dat (load_dirichlet_tables :180-257). */
+int specter_plan_create(const int n[3], const int c[3], const int o[3], const double len[3],
+                        const char *tdir, int precision, specter_plan **out);
+int specter_plan_destroy(specter_plan *plan);            /* fcgram_destroy_plan :147-177 */
+/* info[0..7] = nx, ny, nz, Cz, oz, nx/2+1, padded kx stride, precision */
+int specter_plan_info(const specter_plan *plan, int info[8]);
+/* kx[nx/2+1], ky[ny], kz[nz], z[nz] (the kes and grid modules), dir[Cz*oz] Fortran order */
+int specter_plan_arrays(const specter_plan *plan, double *kx, double *ky, double *kz, double *z, double *dir);
+int specter_plan_synchronize(specter_plan *plan);
+/* the plan's cudaStream_t, for callers that record CUDA events around library work */
+int specter_plan_stream(specter_plan *plan, void **stream);
+
+/* ---- fields (device-resident arrays of the plan's precision) */
+int specter_field_create(specter_plan *plan, int kind, specter_field **out);
+int specter_field_destroy(specter_field *f);
+int specter_field_upload(specter_field *f, const void *host);    /* reference layout */
+int specter_field_download(const specter_field *f, void *host);  /* reference layout */
+int specter_field_copy(specter_field *dst, const specter_field *src);
+int specter_field_zero(specter_field *f);
+/* upload/download of a contiguous batch of host rows is the same call with a pinned buffer;
+ * the device pointer of a field, for interop (layout: see the design doc, kx fastest) */
+int specter_field_device_ptr(specter_field *f, void **ptr, long long *bytes);
+
+/* ---- fftp (src/fftp/fftp.fpp) */
+int specter_fftp3d_real_to_complex(specter_plan *plan, const specter_field *in, specter_field *out);   /* :388-425 */
+int specter_fftp3d_complex_to_real(specter_plan *plan, specter_field *in, specter_field *out);         /* :789-821, in destroyed */
+int specter_fftp2d_real_to_complex_xy(specter_plan *plan, const specter_field *in, specter_field *out);/* :428-524 */
+int specter_fftp2d_complex_to_real_xy(specter_plan *plan, const specter_field *in, specter_field *out);/* :824-919 */
+int specter_fftp1d_real_to_complex_z(specter_plan *plan, specter_field *inout);                       /* :720-786 */
+int specter_fftp1d_complex_to_real_z(specter_plan *plan, specter_field *inout);                       /* :1060-1094 */
+
+/* ---- pseudo (src/pseudo/pseudospec_hd.f90, pseudospec_phd.f90) */
+int specter_derivk(specter_plan *plan, const specter_field *a, specter_field *b, int dir);           /* hd :28-94 */
+int specter_laplak(specter_plan *plan, const specter_field *a, specter_field *b);                    /* hd :97-127 */
+int specter_curlk(specter_plan *plan, const specter_field *a, const specter_field *b,
+                  specter_field *c, int dir);                                                        /* hd :130-206 */
+int specter_gradre(specter_plan *plan, const specter_field *a, const specter_field *b,
+                   const specter_field *c, specter_field *d, specter_field *e, specter_field *f);    /* hd :209-319 */
+int specter_advect(specter_plan *plan, const specter_field *a, const specter_field *b,
+                   const specter_field *c, const specter_field *d, specter_field *e);                /* phd :23-113 */
+int specter_fc_filter(specter_plan *plan, specter_field *a);                                         /* hd :1082-1115 */
+int specter_energy(specter_plan *plan, const specter_field *a, const specter_field *b,
+                   const specter_field *c, int kin, double *out);                                    /* hd :405-635 */
+int specter_helicity(specter_plan *plan, const specter_field *a, const specter_field *b,
+                     const specter_field *c, double *out);                                           /* hd :638-775 */
+int specter_cross(specter_plan *plan, const specter_field *a, const specter_field *b,
+                  const specter_field *c, const specter_field *d, const specter_field *e,
+                  const specter_field *f, int kin, double *out);                                     /* hd :778-940 */
+int specter_divergence(specter_plan *plan, const specter_field *a, const specter_field *b,
+                       const specter_field *c, double *out);                                         /* hd :1118-1235 */
+int specter_variance(specter_plan *plan, const specter_field *a, int kin, double *out);              /* phd :116-196 */
+int specter_product(specter_plan *plan, const specter_field *a, const specter_field *b, double *out);/* phd :199-272 */
+
+/* ---- boundary (src/boundary/boundary_mod.fpp, vboundary.f90, sboundary.f90) */
+int specter_bouncheck_z(specter_plan *plan, const specter_field *a, const specter_field *b,
+                        double *bot, double *top);                                                   /* boundary_mod :681-801 (b may be NULL) */
+int specter_sol_project(specter_plan *plan, specter_field *a, specter_field *b, specter_field *c,
+                        specter_field *d, int bctarget, int bczsta, int bczend);                     /* boundary_mod :197-402 */
+int specter_v_imposebc_and_project(specter_plan *plan, specter_field *vx, specter_field *vy,
+                                   specter_field *vz, specter_field *pr, int rki, int ord,
+                                   const double v_zsta[2], const double v_zend[2]);                  /* vboundary :67-151 */
+int specter_s_imposebc(specter_plan *plan, specter_field *th);                                       /* sboundary :67-119 */
+
+/* ---- solver: the RK loop (src/specter.fpp:1142-1161) with the stage bodies
+ *      src/include/hd/hd_rkstep2.f90 and src/include/bouss/bouss_rkstep2.f90. */
+typedef struct specter_solver_params {
+    int solver;              /* SPECTER_HD or SPECTER_BOUSS */
+    int ord;                 /* RK order (parameter ORD) */
+    double dt, nu, kappa;    /* &parameter dt, &velocity nu, &scalar kappa */
+    double gama, xmom, xtemp;/* &boussinesq; xmom and xtemp are multiplied by gama (specter.fpp:490-491) */
+    double v_zsta[2];        /* &velbound vxzsta, vyzsta */
+    double v_zend[2];        /* &velbound vxzend, vyzend */
+    int fused;               /* 1: fused GB300 stage kernels; 0: the reference call sequence */
+} specter_solver_params;
+
+int specter_solver_create(specter_plan *plan, const specter_solver_params *p, specter_solver **out);
+int specter_solver_destroy(specter_solver *s);
+/* state handles owned by the solver: vx, vy, vz, th (NULL for HD), pr */
+int specter_solver_fields(specter_solver *s, specter_field **vx, specter_field **vy,
+                          specter_field **vz, specter_field **th, specter_field **pr);
+int specter_solver_step(specter_solver *s, int nsteps);      /* rkstep1 + ORD stages per step */
+int specter_solver_stage(specter_solver *s, int o);          /* one stage o (rkstep2 body) */
+/* checks the state for non-finite values (SPECTER_ERR_NONFINITE if any) */
+int specter_solver_check(specter_solver *s);
+
+/* ---- timers: out = {ffttime, tratime, comtime, conttime, tottime, stages} in seconds,
+ *      accumulated from CUDA events (the reference's fftp_mod.fpp:32-37 accumulators) */
+int specter_timers(specter_plan *plan, double out[6]);
+int specter_timers_reset(specter_plan *plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

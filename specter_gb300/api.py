@@ -1,0 +1,313 @@
+"""Host-side mirror of SPECTER's fftp / pseudo / boundary module interfaces over the C ABI.
+
+Names, argument order and meaning follow the reference routines (src/fftp/fftp.fpp,
+src/pseudo/pseudospec_hd.f90, pseudospec_phd.f90, src/boundary/*.f90); the MPI communicator
+argument has no counterpart.  Host arrays use the reference layouts:
+  complex spectral / mixed fields: numpy (nx/2+1, ny, nz) C order  == Fortran C(nz, ny, nx/2+1)
+  real physical fields:            numpy (nz, ny, nx)     C order  == Fortran R(nx, ny, nz)
+in the plan's precision (complex128/float64 for FP64, complex64/float32 for FP32).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from ._lib import SolverParams, SpecterError, check, load
+
+TABLES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tables")
+FP64, FP32 = 0, 1
+COMPLEX, REAL = 0, 1
+HD, BOUSS = 0, 1
+
+
+def _pd(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Plan:
+    """fcgram_create_plan (src/fftp/fcgram_mod.f90:49-144) plus the grid / kes setup
+    (src/specter.fpp:683-800).  n = (nx, ny, nz) with nz the total z size (physical + Cz)."""
+
+    def __init__(self, n, c=(0, 0, 25), o=(0, 0, 5), lengths=(1.0, 1.0, 1.0), tdir=None, precision=FP64):
+        L = load()
+        self._L = L
+        h = C.c_void_p()
+        n3 = (C.c_int * 3)(*n)
+        c3 = (C.c_int * 3)(*c)
+        o3 = (C.c_int * 3)(*o)
+        l3 = (C.c_double * 3)(*lengths)
+        check(L.specter_plan_create(n3, c3, o3, l3, (tdir or TABLES).encode(), int(precision), C.byref(h)))
+        self.h = h
+        info = (C.c_int * 8)()
+        check(L.specter_plan_info(h, info))
+        self.nx, self.ny, self.nz, self.cz, self.oz, self.nxh, self.ldx, self.precision = list(info)
+        self.nzp = self.nz - self.cz
+        self.lengths = tuple(lengths)
+        self.rdtype = np.float64 if self.precision == FP64 else np.float32
+        self.cdtype = np.complex128 if self.precision == FP64 else np.complex64
+        kx, ky, kz, z = np.zeros(self.nxh), np.zeros(self.ny), np.zeros(self.nz), np.zeros(self.nz)
+        d = np.zeros(self.cz * self.oz)
+        check(L.specter_plan_arrays(h, _pd(kx), _pd(ky), _pd(kz), _pd(z), _pd(d)))
+        self.kx, self.ky, self.kz, self.z = kx, ky, kz, z
+        self.dir = d.reshape(self.oz, self.cz).T.copy()
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.specter_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def sshape(self):
+        return (self.nxh, self.ny, self.nz)
+
+    @property
+    def rshape(self):
+        return (self.nz, self.ny, self.nx)
+
+    def field(self, kind=COMPLEX, data=None) -> "Field":
+        f = Field(self, kind)
+        if data is not None:
+            f.upload(data)
+        return f
+
+    def synchronize(self):
+        check(self._L.specter_plan_synchronize(self.h))
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(self._L.specter_plan_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+    def timers(self):
+        out = (C.c_double * 6)()
+        check(self._L.specter_timers(self.h, out))
+        return list(out)
+
+
+class Field:
+    """Device-resident field handle (complex spectral/mixed or real physical)."""
+
+    def __init__(self, plan: Plan, kind=COMPLEX):
+        self.plan = plan
+        self.kind = kind
+        h = C.c_void_p()
+        check(plan._L.specter_field_create(plan.h, kind, C.byref(h)))
+        self.h = h
+        self._owned = True
+
+    @classmethod
+    def _borrow(cls, plan, h, kind=COMPLEX):
+        f = cls.__new__(cls)
+        f.plan, f.kind, f.h, f._owned = plan, kind, h, False
+        return f
+
+    def close(self):
+        if getattr(self, "_owned", False) and getattr(self, "h", None):
+            self.plan._L.specter_field_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def shape(self):
+        return self.plan.sshape if self.kind == COMPLEX else self.plan.rshape
+
+    @property
+    def dtype(self):
+        return self.plan.cdtype if self.kind == COMPLEX else self.plan.rdtype
+
+    def upload(self, a):
+        a = np.ascontiguousarray(a, dtype=self.dtype)
+        if a.shape != self.shape:
+            raise ValueError(f"expected shape {self.shape}, got {a.shape}")
+        check(self.plan._L.specter_field_upload(self.h, a.ctypes.data_as(C.c_void_p)))
+        self.plan.synchronize()
+        return self
+
+    def download(self, out=None):
+        if out is None:
+            out = np.empty(self.shape, self.dtype)
+        check(self.plan._L.specter_field_download(self.h, out.ctypes.data_as(C.c_void_p)))
+        return out
+
+    def copy_from(self, other: "Field"):
+        check(self.plan._L.specter_field_copy(self.h, other.h))
+        return self
+
+    def zero(self):
+        check(self.plan._L.specter_field_zero(self.h))
+        return self
+
+
+def _L(plan):
+    return plan._L
+
+
+# ---------------------------------------------------------------- fftp (src/fftp/fftp.fpp)
+def fftp3d_real_to_complex(plan, inp: Field, out: Field):
+    check(_L(plan).specter_fftp3d_real_to_complex(plan.h, inp.h, out.h))
+
+
+def fftp3d_complex_to_real(plan, inp: Field, out: Field):
+    """The input is destroyed, as in the reference (fftp.fpp:812)."""
+    check(_L(plan).specter_fftp3d_complex_to_real(plan.h, inp.h, out.h))
+
+
+def fftp2d_real_to_complex_xy(plan, inp, out):
+    check(_L(plan).specter_fftp2d_real_to_complex_xy(plan.h, inp.h, out.h))
+
+
+def fftp2d_complex_to_real_xy(plan, inp, out):
+    check(_L(plan).specter_fftp2d_complex_to_real_xy(plan.h, inp.h, out.h))
+
+
+def fftp1d_real_to_complex_z(plan, inout):
+    check(_L(plan).specter_fftp1d_real_to_complex_z(plan.h, inout.h))
+
+
+def fftp1d_complex_to_real_z(plan, inout):
+    check(_L(plan).specter_fftp1d_complex_to_real_z(plan.h, inout.h))
+
+
+# ---------------------------------------------------------------- pseudo
+def derivk(plan, a, b, dir):
+    check(_L(plan).specter_derivk(plan.h, a.h, b.h, dir))
+
+
+def laplak(plan, a, b):
+    check(_L(plan).specter_laplak(plan.h, a.h, b.h))
+
+
+def curlk(plan, a, b, c, dir):
+    check(_L(plan).specter_curlk(plan.h, a.h, b.h, c.h, dir))
+
+
+def gradre(plan, a, b, c, d, e, f):
+    check(_L(plan).specter_gradre(plan.h, a.h, b.h, c.h, d.h, e.h, f.h))
+
+
+def advect(plan, a, b, c, d, e):
+    check(_L(plan).specter_advect(plan.h, a.h, b.h, c.h, d.h, e.h))
+
+
+def fc_filter(plan, a):
+    check(_L(plan).specter_fc_filter(plan.h, a.h))
+
+
+def _scalar(fn, *args):
+    out = C.c_double()
+    check(fn(*args, C.byref(out)))
+    return out.value
+
+
+def energy(plan, a, b, c, kin):
+    return _scalar(_L(plan).specter_energy, plan.h, a.h, b.h, c.h, kin)
+
+
+def helicity(plan, a, b, c):
+    return _scalar(_L(plan).specter_helicity, plan.h, a.h, b.h, c.h)
+
+
+def cross(plan, a, b, c, d, e, f, kin):
+    return _scalar(_L(plan).specter_cross, plan.h, a.h, b.h, c.h, d.h, e.h, f.h, kin)
+
+
+def divergence(plan, a, b, c):
+    return _scalar(_L(plan).specter_divergence, plan.h, a.h, b.h, c.h)
+
+
+def variance(plan, a, kin):
+    return _scalar(_L(plan).specter_variance, plan.h, a.h, kin)
+
+
+def product(plan, a, b):
+    return _scalar(_L(plan).specter_product, plan.h, a.h, b.h)
+
+
+# ---------------------------------------------------------------- boundary
+def bouncheck_z(plan, a, b=None):
+    bot, top = C.c_double(), C.c_double()
+    check(_L(plan).specter_bouncheck_z(plan.h, a.h, b.h if b is not None else None, C.byref(bot), C.byref(top)))
+    return bot.value, top.value
+
+
+def sol_project(plan, a, b, c, d, bctarget=1, bczsta=0, bczend=0):
+    check(_L(plan).specter_sol_project(plan.h, a.h, b.h, c.h, d.h, bctarget, bczsta, bczend))
+
+
+def v_imposebc_and_project(plan, vx, vy, vz, pr, rki, ord, v_zsta=(0.0, 0.0), v_zend=(0.0, 0.0)):
+    zs = (C.c_double * 2)(*v_zsta)
+    ze = (C.c_double * 2)(*v_zend)
+    check(_L(plan).specter_v_imposebc_and_project(plan.h, vx.h, vy.h, vz.h, pr.h, rki, ord, zs, ze))
+
+
+def s_imposebc(plan, th):
+    check(_L(plan).specter_s_imposebc(plan.h, th.h))
+
+
+# ---------------------------------------------------------------- solver (RK loop)
+class Solver:
+    """The RK loop of src/specter.fpp:1142-1161 with the HD or BOUSS stage body.
+
+    fused=True runs the GB300 fused stage kernels; fused=False runs the reference's call
+    sequence (gradre, fc_filter, laplak, update, v_imposebc_and_project, ...) on the GPU."""
+
+    def __init__(self, plan: Plan, solver=HD, ord=2, dt=1e-4, nu=1e-3, kappa=0.0, gama=1.0,
+                 xmom=1.0, xtemp=1.0, v_zsta=(0.0, 0.0), v_zend=(0.0, 0.0), fused=True):
+        self.plan = plan
+        p = SolverParams()
+        p.solver, p.ord, p.dt, p.nu, p.kappa = solver, ord, dt, nu, kappa
+        p.gama, p.xmom, p.xtemp = gama, xmom, xtemp
+        p.v_zsta[0], p.v_zsta[1] = v_zsta
+        p.v_zend[0], p.v_zend[1] = v_zend
+        p.fused = 1 if fused else 0
+        self.params = p
+        h = C.c_void_p()
+        check(_L(plan).specter_solver_create(plan.h, C.byref(p), C.byref(h)))
+        self.h = h
+        ptrs = [C.c_void_p() for _ in range(5)]
+        check(_L(plan).specter_solver_fields(h, *[C.byref(x) for x in ptrs]))
+        vx, vy, vz, th, pr = ptrs
+        self.vx, self.vy, self.vz = (Field._borrow(plan, x) for x in (vx, vy, vz))
+        self.th = Field._borrow(plan, th) if th.value else None
+        self.pr = Field._borrow(plan, pr)
+
+    def close(self):
+        if getattr(self, "h", None):
+            _L(self.plan).specter_solver_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def state(self):
+        return [f for f in (self.vx, self.vy, self.vz, self.th) if f is not None] + [self.pr]
+
+    def step(self, n=1):
+        check(_L(self.plan).specter_solver_step(self.h, n))
+
+    def stage(self, o):
+        check(_L(self.plan).specter_solver_stage(self.h, o))
+
+    def check(self):
+        check(_L(self.plan).specter_solver_check(self.h))
+
+
+__all__ = [n for n in dir() if not n.startswith("_")] + ["SpecterError"]

@@ -1,0 +1,514 @@
+// C ABI (include/specter_gpu.h): handles, reference-layout conversion, dispatch on precision.
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/specter_gpu.h"
+#include "fused.h"
+#include "ops.h"
+
+using namespace sg;
+
+namespace sg {
+const char *last_error();
+}
+
+// A plan stays alive while fields or solvers made from it exist: specter_plan_destroy only
+// drops the caller's reference, so handles may be released in any order.
+struct specter_plan {
+    Plan *p;
+    int refs;
+};
+
+static void plan_release(specter_plan *pl) {
+    if (--pl->refs == 0) {
+        plan_destroy(pl->p);
+        delete pl;
+    }
+}
+
+struct specter_field {
+    specter_plan *plan;
+    int kind;
+    void *d;
+    size_t bytes;
+};
+
+struct specter_solver {
+    specter_plan *plan;
+    StageParams sp;
+    int fused;
+    specter_field *v[4];   // vx, vy, vz, th
+    specter_field *pr;
+    void *cold[4];         // RK storage C1, C2, C3, C7
+    FusedState *fs;
+};
+
+#define CHECK_PLAN(pl)                                                         \
+    do {                                                                       \
+        if (!(pl) || !(pl)->p) { set_error("null plan"); return SPECTER_ERR_ARG; } \
+    } while (0)
+
+static int need(const specter_field *f, const specter_plan *pl, int kind) {
+    if (!f || !f->d) { set_error("null field"); return SPECTER_ERR_ARG; }
+    if (f->plan != pl) { set_error("field belongs to a different plan"); return SPECTER_ERR_STATE; }
+    if (f->kind != kind) { set_error(kind == SPECTER_COMPLEX ? "expected a complex field" : "expected a real field"); return SPECTER_ERR_ARG; }
+    return SPECTER_OK;
+}
+#define NEED(f, k)                                  \
+    do {                                            \
+        int _s = need((f), plan, (k));              \
+        if (_s) return _s;                          \
+    } while (0)
+
+#define DISPATCH(plan, call) ((plan)->p->prec == FP64 ? Ops<double>::call : Ops<float>::call)
+
+extern "C" {
+
+const char *specter_last_error(void) { return sg::last_error(); }
+int specter_version(void) { return 100; }
+
+int specter_device_count(int *count) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) { *count = 0; set_error(cudaGetErrorString(e)); return SPECTER_ERR_CUDA; }
+    *count = n;
+    return SPECTER_OK;
+}
+
+int specter_plan_create(const int n[3], const int c[3], const int o[3], const double len[3],
+                        const char *tdir, int precision, specter_plan **out) {
+    if (!n || !c || !o || !len || !out) { set_error("null argument"); return SPECTER_ERR_ARG; }
+    *out = nullptr;
+    int dev = 0;
+    if (cudaGetDeviceCount(&dev) != cudaSuccess || dev < 1) {
+        set_error("no CUDA device: the GB300 path has no CPU fallback");
+        return SPECTER_ERR_CUDA;
+    }
+    Plan *p = nullptr;
+    int st = plan_create(&p, n, c, o, len, tdir, precision);
+    if (st) return st;
+    specter_plan *h = new (std::nothrow) specter_plan{p, 1};
+    *out = h;
+    return SPECTER_OK;
+}
+
+int specter_plan_destroy(specter_plan *plan) {
+    if (!plan) return SPECTER_OK;
+    plan_release(plan);
+    return SPECTER_OK;
+}
+
+int specter_plan_info(const specter_plan *plan, int info[8]) {
+    CHECK_PLAN(plan);
+    const Plan &P = *plan->p;
+    int v[8] = {P.nx, P.ny, P.nz, P.cz, P.oz, P.nxh, P.ldx, (int)P.prec};
+    memcpy(info, v, sizeof v);
+    return SPECTER_OK;
+}
+
+int specter_plan_arrays(const specter_plan *plan, double *kx, double *ky, double *kz, double *z, double *dir) {
+    CHECK_PLAN(plan);
+    const Plan &P = *plan->p;
+    if (kx) memcpy(kx, P.kx.data(), sizeof(double) * P.nxh);
+    if (ky) memcpy(ky, P.ky.data(), sizeof(double) * P.ny);
+    if (kz) memcpy(kz, P.kz.data(), sizeof(double) * P.nz);
+    if (z) memcpy(z, P.z.data(), sizeof(double) * P.nz);
+    if (dir) memcpy(dir, P.dir.data(), sizeof(double) * P.dir.size());
+    return SPECTER_OK;
+}
+
+int specter_plan_synchronize(specter_plan *plan) {
+    CHECK_PLAN(plan);
+    cudaError_t e = cudaStreamSynchronize(plan->p->stream);
+    if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return SPECTER_ERR_CUDA; }
+    return SPECTER_OK;
+}
+
+int specter_plan_stream(specter_plan *plan, void **stream) {
+    CHECK_PLAN(plan);
+    *stream = (void *)plan->p->stream;
+    return SPECTER_OK;
+}
+
+// ------------------------------------------------------------------ fields
+
+int specter_field_create(specter_plan *plan, int kind, specter_field **out) {
+    CHECK_PLAN(plan);
+    if (kind != SPECTER_COMPLEX && kind != SPECTER_REAL) { set_error("bad field kind"); return SPECTER_ERR_ARG; }
+    const Plan &P = *plan->p;
+    size_t bytes = kind == SPECTER_COMPLEX ? P.field_bytes() : P.real_elems() * P.rel();
+    void *d = nullptr;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) { cudaGetLastError(); set_error("cudaMalloc failed for a field"); return SPECTER_ERR_OOM; }
+    cudaMemsetAsync(d, 0, bytes, P.stream);
+    *out = new specter_field{plan, kind, d, bytes};
+    plan->refs++;
+    return SPECTER_OK;
+}
+
+int specter_field_destroy(specter_field *f) {
+    if (!f) return SPECTER_OK;
+    cudaStreamSynchronize(f->plan->p->stream);
+    if (f->d) cudaFree(f->d);
+    specter_plan *pl = f->plan;
+    delete f;
+    plan_release(pl);
+    return SPECTER_OK;
+}
+
+}  // extern "C"
+
+// reference C(nz, ny, nxh) [z fastest]  <->  device [(z*ny + ky)*ldx + kx]
+template <typename V>
+__global__ void k_ref_to_dev(const V *__restrict__ h, V *__restrict__ d, int nz, int ny, int nxh, int ldx) {
+    __shared__ V tile[32][33];
+    const int ky = blockIdx.z;
+    const int z0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {  // r indexes kx, threadIdx.x indexes z
+        const int kx = k0 + r, z = z0 + threadIdx.x;
+        if (kx < nxh && z < nz) tile[r][threadIdx.x] = h[((size_t)kx * ny + ky) * nz + z];
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {  // r indexes z, threadIdx.x indexes kx
+        const int z = z0 + r, kx = k0 + threadIdx.x;
+        if (kx < nxh && z < nz) d[((size_t)z * ny + ky) * ldx + kx] = tile[threadIdx.x][r];
+    }
+}
+
+template <typename V>
+__global__ void k_dev_to_ref(const V *__restrict__ d, V *__restrict__ h, int nz, int ny, int nxh, int ldx) {
+    __shared__ V tile[32][33];
+    const int ky = blockIdx.z;
+    const int z0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {  // r indexes z, threadIdx.x indexes kx
+        const int z = z0 + r, kx = k0 + threadIdx.x;
+        if (kx < nxh && z < nz) tile[r][threadIdx.x] = d[((size_t)z * ny + ky) * ldx + kx];
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {  // r indexes kx, threadIdx.x indexes z
+        const int kx = k0 + r, z = z0 + threadIdx.x;
+        if (kx < nxh && z < nz) h[((size_t)kx * ny + ky) * nz + z] = tile[threadIdx.x][r];
+    }
+}
+
+static int staging(Plan &P, void **buf) {
+    // staging slot for reference-layout data: one more scratch field
+    *buf = P.scratch_field(23);
+    if (!*buf) { set_error("out of device memory (staging)"); return SPECTER_ERR_OOM; }
+    return SPECTER_OK;
+}
+
+static int convert(Plan &P, const void *src, void *dst, bool to_dev) {
+    dim3 grid(cdiv(P.nz, 32), cdiv(P.nxh, 32), P.ny), block(32, 8);
+    if (P.prec == FP64) {
+        if (to_dev) k_ref_to_dev<double2><<<grid, block, 0, P.stream>>>((const double2 *)src, (double2 *)dst, P.nz, P.ny, P.nxh, P.ldx);
+        else k_dev_to_ref<double2><<<grid, block, 0, P.stream>>>((const double2 *)src, (double2 *)dst, P.nz, P.ny, P.nxh, P.ldx);
+    } else {
+        if (to_dev) k_ref_to_dev<float2><<<grid, block, 0, P.stream>>>((const float2 *)src, (float2 *)dst, P.nz, P.ny, P.nxh, P.ldx);
+        else k_dev_to_ref<float2><<<grid, block, 0, P.stream>>>((const float2 *)src, (float2 *)dst, P.nz, P.ny, P.nxh, P.ldx);
+    }
+    return check_launch("layout conversion");
+}
+
+extern "C" {
+
+int specter_field_upload(specter_field *f, const void *host) {
+    if (!f || !host) { set_error("null argument"); return SPECTER_ERR_ARG; }
+    Plan &P = *f->plan->p;
+    if (f->kind == SPECTER_REAL) {
+        if (cudaMemcpyAsync(f->d, host, f->bytes, cudaMemcpyHostToDevice, P.stream) != cudaSuccess) return check_launch("upload");
+        return SPECTER_OK;
+    }
+    void *stg;
+    int st = staging(P, &stg);
+    if (st) return st;
+    const size_t nbytes = (size_t)P.nz * P.ny * P.nxh * P.elt();
+    if (cudaMemcpyAsync(stg, host, nbytes, cudaMemcpyHostToDevice, P.stream) != cudaSuccess) return check_launch("upload");
+    return convert(P, stg, f->d, true);
+}
+
+int specter_field_download(const specter_field *f, void *host) {
+    if (!f || !host) { set_error("null argument"); return SPECTER_ERR_ARG; }
+    Plan &P = *f->plan->p;
+    if (f->kind == SPECTER_REAL) {
+        if (cudaMemcpyAsync(host, f->d, f->bytes, cudaMemcpyDeviceToHost, P.stream) != cudaSuccess) return check_launch("download");
+    } else {
+        void *stg;
+        int st = staging(P, &stg);
+        if (st) return st;
+        if ((st = convert(P, f->d, stg, false))) return st;
+        const size_t nbytes = (size_t)P.nz * P.ny * P.nxh * P.elt();
+        if (cudaMemcpyAsync(host, stg, nbytes, cudaMemcpyDeviceToHost, P.stream) != cudaSuccess) return check_launch("download");
+    }
+    if (cudaStreamSynchronize(P.stream) != cudaSuccess) return check_launch("download");
+    return SPECTER_OK;
+}
+
+int specter_field_copy(specter_field *dst, const specter_field *src) {
+    if (!dst || !src || dst->plan != src->plan || dst->kind != src->kind) { set_error("incompatible fields"); return SPECTER_ERR_ARG; }
+    cudaMemcpyAsync(dst->d, src->d, dst->bytes, cudaMemcpyDeviceToDevice, dst->plan->p->stream);
+    return check_launch("field copy");
+}
+
+int specter_field_zero(specter_field *f) {
+    if (!f) { set_error("null field"); return SPECTER_ERR_ARG; }
+    cudaMemsetAsync(f->d, 0, f->bytes, f->plan->p->stream);
+    return check_launch("field zero");
+}
+
+int specter_field_device_ptr(specter_field *f, void **ptr, long long *bytes) {
+    if (!f) { set_error("null field"); return SPECTER_ERR_ARG; }
+    *ptr = f->d;
+    if (bytes) *bytes = (long long)f->bytes;
+    return SPECTER_OK;
+}
+
+// ------------------------------------------------------------------ fftp
+
+int specter_fftp3d_real_to_complex(specter_plan *plan, const specter_field *in, specter_field *out) {
+    CHECK_PLAN(plan); NEED(in, SPECTER_REAL); NEED(out, SPECTER_COMPLEX);
+    return DISPATCH(plan, fftp3d_r2c(*plan->p, in->d, out->d));
+}
+int specter_fftp3d_complex_to_real(specter_plan *plan, specter_field *in, specter_field *out) {
+    CHECK_PLAN(plan); NEED(in, SPECTER_COMPLEX); NEED(out, SPECTER_REAL);
+    return DISPATCH(plan, fftp3d_c2r(*plan->p, in->d, out->d));
+}
+int specter_fftp2d_real_to_complex_xy(specter_plan *plan, const specter_field *in, specter_field *out) {
+    CHECK_PLAN(plan); NEED(in, SPECTER_REAL); NEED(out, SPECTER_COMPLEX);
+    return DISPATCH(plan, fftp2d_r2c_xy(*plan->p, in->d, out->d));
+}
+int specter_fftp2d_complex_to_real_xy(specter_plan *plan, const specter_field *in, specter_field *out) {
+    CHECK_PLAN(plan); NEED(in, SPECTER_COMPLEX); NEED(out, SPECTER_REAL);
+    return DISPATCH(plan, fftp2d_c2r_xy(*plan->p, in->d, out->d));
+}
+int specter_fftp1d_real_to_complex_z(specter_plan *plan, specter_field *inout) {
+    CHECK_PLAN(plan); NEED(inout, SPECTER_COMPLEX);
+    return DISPATCH(plan, fftp1d_r2c_z(*plan->p, inout->d));
+}
+int specter_fftp1d_complex_to_real_z(specter_plan *plan, specter_field *inout) {
+    CHECK_PLAN(plan); NEED(inout, SPECTER_COMPLEX);
+    return DISPATCH(plan, fftp1d_c2r_z(*plan->p, inout->d));
+}
+
+// ------------------------------------------------------------------ pseudo
+
+int specter_derivk(specter_plan *plan, const specter_field *a, specter_field *b, int dir) {
+    CHECK_PLAN(plan); NEED(a, SPECTER_COMPLEX); NEED(b, SPECTER_COMPLEX);
+    return DISPATCH(plan, derivk(*plan->p, a->d, b->d, dir));
+}
+int specter_laplak(specter_plan *plan, const specter_field *a, specter_field *b) {
+    CHECK_PLAN(plan); NEED(a, SPECTER_COMPLEX); NEED(b, SPECTER_COMPLEX);
+    return DISPATCH(plan, laplak(*plan->p, a->d, b->d));
+}
+int specter_curlk(specter_plan *plan, const specter_field *a, const specter_field *b, specter_field *c, int dir) {
+    CHECK_PLAN(plan); NEED(a, SPECTER_COMPLEX); NEED(b, SPECTER_COMPLEX); NEED(c, SPECTER_COMPLEX);
+    return DISPATCH(plan, curlk(*plan->p, a->d, b->d, c->d, dir));
+}
+int specter_gradre(specter_plan *plan, const specter_field *a, const specter_field *b, const specter_field *c,
+                   specter_field *d, specter_field *e, specter_field *f) {
+    CHECK_PLAN(plan);
+    NEED(a, SPECTER_COMPLEX); NEED(b, SPECTER_COMPLEX); NEED(c, SPECTER_COMPLEX);
+    NEED(d, SPECTER_COMPLEX); NEED(e, SPECTER_COMPLEX); NEED(f, SPECTER_COMPLEX);
+    const void *v[3] = {a->d, b->d, c->d};
+    void *out[4] = {d->d, e->d, f->d, nullptr};
+    return DISPATCH(plan, nonlinear(*plan->p, v, nullptr, out, 0, 3));
+}
+int specter_advect(specter_plan *plan, const specter_field *a, const specter_field *b, const specter_field *c,
+                   const specter_field *d, specter_field *e) {
+    CHECK_PLAN(plan);
+    NEED(a, SPECTER_COMPLEX); NEED(b, SPECTER_COMPLEX); NEED(c, SPECTER_COMPLEX);
+    NEED(d, SPECTER_COMPLEX); NEED(e, SPECTER_COMPLEX);
+    const void *v[3] = {a->d, b->d, c->d};
+    void *out[4] = {nullptr, nullptr, nullptr, e->d};
+    return DISPATCH(plan, nonlinear(*plan->p, v, d->d, out, 3, 4));
+}
+int specter_fc_filter(specter_plan *plan, specter_field *a) {
+    CHECK_PLAN(plan); NEED(a, SPECTER_COMPLEX);
+    return DISPATCH(plan, fc_filter(*plan->p, a->d));
+}
+int specter_energy(specter_plan *plan, const specter_field *a, const specter_field *b, const specter_field *c,
+                   int kin, double *out) {
+    CHECK_PLAN(plan); NEED(a, SPECTER_COMPLEX); NEED(b, SPECTER_COMPLEX); NEED(c, SPECTER_COMPLEX);
+    return DISPATCH(plan, energy(*plan->p, a->d, b->d, c->d, kin, out));
+}
+int specter_helicity(specter_plan *plan, const specter_field *a, const specter_field *b, const specter_field *c,
+                     double *out) {
+    CHECK_PLAN(plan); NEED(a, SPECTER_COMPLEX); NEED(b, SPECTER_COMPLEX); NEED(c, SPECTER_COMPLEX);
+    return DISPATCH(plan, helicity(*plan->p, a->d, b->d, c->d, out));
+}
+int specter_cross(specter_plan *plan, const specter_field *a, const specter_field *b, const specter_field *c,
+                  const specter_field *d, const specter_field *e, const specter_field *f, int kin, double *out) {
+    CHECK_PLAN(plan);
+    NEED(a, SPECTER_COMPLEX); NEED(b, SPECTER_COMPLEX); NEED(c, SPECTER_COMPLEX);
+    NEED(d, SPECTER_COMPLEX); NEED(e, SPECTER_COMPLEX); NEED(f, SPECTER_COMPLEX);
+    const void *A[3] = {a->d, b->d, c->d}, *B[3] = {d->d, e->d, f->d};
+    return DISPATCH(plan, cross(*plan->p, A, B, kin, out));
+}
+int specter_divergence(specter_plan *plan, const specter_field *a, const specter_field *b, const specter_field *c,
+                       double *out) {
+    CHECK_PLAN(plan); NEED(a, SPECTER_COMPLEX); NEED(b, SPECTER_COMPLEX); NEED(c, SPECTER_COMPLEX);
+    return DISPATCH(plan, divergence(*plan->p, a->d, b->d, c->d, out));
+}
+int specter_variance(specter_plan *plan, const specter_field *a, int kin, double *out) {
+    CHECK_PLAN(plan); NEED(a, SPECTER_COMPLEX);
+    return DISPATCH(plan, variance(*plan->p, a->d, kin, out));
+}
+int specter_product(specter_plan *plan, const specter_field *a, const specter_field *b, double *out) {
+    CHECK_PLAN(plan); NEED(a, SPECTER_COMPLEX); NEED(b, SPECTER_COMPLEX);
+    return DISPATCH(plan, product(*plan->p, a->d, b->d, out));
+}
+
+// ------------------------------------------------------------------ boundary
+
+int specter_bouncheck_z(specter_plan *plan, const specter_field *a, const specter_field *b, double *bot, double *top) {
+    CHECK_PLAN(plan); NEED(a, SPECTER_COMPLEX);
+    if (b) NEED(b, SPECTER_COMPLEX);
+    return DISPATCH(plan, bouncheck_z(*plan->p, a->d, b ? b->d : nullptr, bot, top));
+}
+int specter_sol_project(specter_plan *plan, specter_field *a, specter_field *b, specter_field *c, specter_field *d,
+                        int bctarget, int bczsta, int bczend) {
+    CHECK_PLAN(plan);
+    NEED(a, SPECTER_COMPLEX); NEED(b, SPECTER_COMPLEX); NEED(c, SPECTER_COMPLEX); NEED(d, SPECTER_COMPLEX);
+    if (bczsta != 0 || bczend != 0) {
+        set_error("[ERROR] Unsupported BC kind in call to sol_project (only homogeneous Dirichlet walls)");
+        return SPECTER_ERR_BC;
+    }
+    return DISPATCH(plan, sol_project(*plan->p, a->d, b->d, c->d, d->d, bctarget));
+}
+int specter_v_imposebc_and_project(specter_plan *plan, specter_field *vx, specter_field *vy, specter_field *vz,
+                                   specter_field *pr, int rki, int ord, const double v_zsta[2], const double v_zend[2]) {
+    CHECK_PLAN(plan);
+    NEED(vx, SPECTER_COMPLEX); NEED(vy, SPECTER_COMPLEX); NEED(vz, SPECTER_COMPLEX); NEED(pr, SPECTER_COMPLEX);
+    const double zero[2] = {0.0, 0.0};
+    return DISPATCH(plan, v_imposebc_and_project(*plan->p, vx->d, vy->d, vz->d, pr->d, rki, ord,
+                                                 v_zsta ? v_zsta : zero, v_zend ? v_zend : zero));
+}
+int specter_s_imposebc(specter_plan *plan, specter_field *th) {
+    CHECK_PLAN(plan); NEED(th, SPECTER_COMPLEX);
+    return DISPATCH(plan, s_imposebc(*plan->p, th->d));
+}
+
+// ------------------------------------------------------------------ solver
+
+int specter_solver_create(specter_plan *plan, const specter_solver_params *p, specter_solver **out) {
+    CHECK_PLAN(plan);
+    if (!p || !out) { set_error("null argument"); return SPECTER_ERR_ARG; }
+    if ((p->solver != SPECTER_HD && p->solver != SPECTER_BOUSS) || p->ord < 1) { set_error("bad solver parameters"); return SPECTER_ERR_ARG; }
+    specter_solver *s = new specter_solver();  // value-initialised: all handles null
+    s->plan = plan;
+    plan->refs++;
+    s->sp.solver = p->solver;
+    s->sp.ord = p->ord;
+    s->sp.dt = p->dt; s->sp.nu = p->nu; s->sp.kappa = p->kappa;
+    s->sp.xmom = p->xmom * p->gama; s->sp.xtemp = p->xtemp * p->gama;
+    s->sp.vzsta[0] = p->v_zsta[0]; s->sp.vzsta[1] = p->v_zsta[1];
+    s->sp.vzend[0] = p->v_zend[0]; s->sp.vzend[1] = p->v_zend[1];
+    s->fused = p->fused;
+    const int nc = p->solver == SPECTER_BOUSS ? 4 : 3;
+    int st = SPECTER_OK;
+    for (int i = 0; i < 4 && !st; i++) {
+        s->v[i] = nullptr;
+        if (i < nc) st = specter_field_create(plan, SPECTER_COMPLEX, &s->v[i]);
+    }
+    if (!st) st = specter_field_create(plan, SPECTER_COMPLEX, &s->pr);
+    for (int i = 0; i < 4 && !st; i++) {
+        s->cold[i] = nullptr;
+        if (i < nc && cudaMalloc(&s->cold[i], plan->p->field_bytes()) != cudaSuccess) { set_error("cudaMalloc failed"); st = SPECTER_ERR_OOM; }
+    }
+    s->fs = nullptr;
+    if (!st && s->fused) st = fused_create(*plan->p, s->sp, &s->fs);
+    if (st) { specter_solver_destroy(s); return st; }
+    *out = s;
+    return SPECTER_OK;
+}
+
+int specter_solver_destroy(specter_solver *s) {
+    if (!s) return SPECTER_OK;
+    cudaStreamSynchronize(s->plan->p->stream);
+    for (int i = 0; i < 4; i++) { specter_field_destroy(s->v[i]); if (s->cold[i]) cudaFree(s->cold[i]); }
+    specter_field_destroy(s->pr);
+    if (s->fs) fused_destroy(s->fs);
+    specter_plan *pl = s->plan;
+    delete s;
+    plan_release(pl);
+    return SPECTER_OK;
+}
+
+int specter_solver_fields(specter_solver *s, specter_field **vx, specter_field **vy, specter_field **vz,
+                          specter_field **th, specter_field **pr) {
+    if (!s) { set_error("null solver"); return SPECTER_ERR_ARG; }
+    if (vx) *vx = s->v[0];
+    if (vy) *vy = s->v[1];
+    if (vz) *vz = s->v[2];
+    if (th) *th = s->v[3];
+    if (pr) *pr = s->pr;
+    return SPECTER_OK;
+}
+
+}  // extern "C"
+
+static int stage_ref(specter_solver *s, int o) {
+    Plan &P = *s->plan->p;
+    void *v[4] = {s->v[0]->d, s->v[1]->d, s->v[2]->d, s->v[3] ? s->v[3]->d : nullptr};
+    const void *C[4] = {s->cold[0], s->cold[1], s->cold[2], s->cold[3]};
+    return P.prec == FP64 ? Ops<double>::stage(P, s->sp, o, v, s->pr->d, C) : Ops<float>::stage(P, s->sp, o, v, s->pr->d, C);
+}
+
+extern "C" {
+
+int specter_solver_stage(specter_solver *s, int o) {
+    if (!s) { set_error("null solver"); return SPECTER_ERR_ARG; }
+    if (o < 1 || o > s->sp.ord) { set_error("stage index o must be in [1, ord]"); return SPECTER_ERR_ARG; }
+    if (s->fused) {
+        void *v[4] = {s->v[0]->d, s->v[1]->d, s->v[2]->d, s->v[3] ? s->v[3]->d : nullptr};
+        const void *C[4] = {s->cold[0], s->cold[1], s->cold[2], s->cold[3]};
+        return fused_stage(*s->plan->p, s->fs, o, v, s->pr->d, C);
+    }
+    return stage_ref(s, o);
+}
+
+int specter_solver_step(specter_solver *s, int nsteps) {
+    if (!s) { set_error("null solver"); return SPECTER_ERR_ARG; }
+    Plan &P = *s->plan->p;
+    const int nc = s->sp.solver == SPECTER_BOUSS ? 4 : 3;
+    for (int t = 0; t < nsteps; t++) {
+        // rkstep1: C_i = v_i (hd_rkstep1.f90:4-6, bouss_rkstep1.f90:4-7)
+        for (int i = 0; i < nc; i++)
+            cudaMemcpyAsync(s->cold[i], s->v[i]->d, P.field_bytes(), cudaMemcpyDeviceToDevice, P.stream);
+        int st = check_launch("rkstep1");
+        if (st) return st;
+        for (int o = s->sp.ord; o >= 1; o--) {
+            st = specter_solver_stage(s, o);
+            if (st) return st;
+        }
+    }
+    return SPECTER_OK;
+}
+
+int specter_solver_check(specter_solver *s) {
+    if (!s) { set_error("null solver"); return SPECTER_ERR_ARG; }
+    Plan &P = *s->plan->p;
+    const int nc = s->sp.solver == SPECTER_BOUSS ? 4 : 3;
+    for (int i = 0; i < nc; i++) {
+        double e = 0.0;
+        int st = P.prec == FP64 ? Ops<double>::variance(P, s->v[i]->d, 1, &e) : Ops<float>::variance(P, s->v[i]->d, 1, &e);
+        if (st) return st;
+        if (!(e == e) || e > 1e300) { set_error("non-finite value in the solver state"); return SPECTER_ERR_NONFINITE; }
+    }
+    return SPECTER_OK;
+}
+
+int specter_timers(specter_plan *plan, double out[6]) {
+    CHECK_PLAN(plan);
+    for (int i = 0; i < 6; i++) out[i] = plan->p->timers[i];
+    return SPECTER_OK;
+}
+
+int specter_timers_reset(specter_plan *plan) {
+    CHECK_PLAN(plan);
+    for (int i = 0; i < 6; i++) plan->p->timers[i] = 0.0;
+    return SPECTER_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,388 @@
+// Pass kernels over the device field layout.
+//
+// Device layout of every complex field (spectral (kz,ky,kx) or mixed (z,ky,kx)):
+//     f[(z*ny + ky)*ldx + kx],  kx fastest, kx < nx/2+1 <= ldx (ldx padded to 8).
+// The reference stores the same arrays z-fastest, C(nz,ny,nx/2+1); with kx fastest
+// every pass is a batched strided FFT whose loads and stores are coalesced along kx,
+// so no global transpose is needed: the x/y/z passes read (TK kx) x (length) tiles.
+// Physical (real) fields use the reference layout r[(z*ny + y)*nx + x].
+#pragma once
+
+#include "fft.cuh"
+#include "plan.h"
+
+namespace sg {
+
+constexpr int kThreads = 256;
+constexpr int kMaxF = 4;  // fields per launch (blockIdx.z)
+
+template <typename T>
+__device__ __forceinline__ size_t fidx(const Geo &g, int z, int ky, int kx) {
+    return ((size_t)z * g.ny + ky) * g.ldx + kx;
+}
+
+// ---------------------------------------------------------------------------------
+// z pass, inverse: out0 = scale * IFFT_z(in) (+ add), out1 = scale * IFFT_z(i kz in).
+// Rows [0, nrows) are written.  fftp1d_complex_to_real_z, src/fftp/fftp.fpp:1060-1094.
+// ---------------------------------------------------------------------------------
+struct ZInvArgs {
+    const void *in[kMaxF];
+    void *out0[kMaxF];
+    void *out1[kMaxF];
+    const void *add[kMaxF];
+    int nrows;
+    int scale_rows;   // rows [0, scale_rows) scaled, the rest copied unscaled
+    double scale;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_z_inverse(Geo g, FFTDesc fd, ZInvArgs a, int TK) {
+    using V = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * TK;
+    const int kx0 = blockIdx.x * TK, ky = blockIdx.y, f = blockIdx.z;
+    const V *in = (const V *)a.in[f];
+    const int nv = min(TK, g.nxh - kx0);
+    for (int pass = 1; pass >= 0; pass--) {  // derivative output first: out0 may alias in
+        V *out = (V *)(pass == 0 ? a.out0[f] : a.out1[f]);
+        if (!out) continue;
+        for (int idx = threadIdx.x; idx < g.nz * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            V v = mk<T>(0, 0);
+            if (c < nv) v = in[fidx<T>(g, k, ky, kx0 + c)];
+            if (pass == 1) v = cimk((T)g.kz[k], v);
+            X[idx] = v;
+        }
+        __syncthreads();
+        V *R = fft_exec<T>(X, Y, TK, fd, +1);
+        const V *add = (const V *)a.add[f];
+        for (int idx = threadIdx.x; idx < a.nrows * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            if (c >= nv) continue;
+            V v = R[idx];
+            if (k < a.scale_rows) v = cscale(v, (T)a.scale);
+            const size_t q = fidx<T>(g, k, ky, kx0 + c);
+            if (pass == 0 && add) v = cadd(v, add[q]);
+            out[q] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// z pass, forward with FC-Gram continuation: rows [0, nzp) are read (times in_scale),
+// rows [nzp, nz) are rebuilt from the first and last d rows with dir = A.Q^T in FP64
+// (src/fftp/fftp.fpp:755-773), then the forward FFT (:780) writes all nz rows.
+// ---------------------------------------------------------------------------------
+struct ZFwdArgs {
+    const void *in[kMaxF];
+    void *out[kMaxF];
+    double in_scale;
+};
+
+template <typename T>
+__device__ __forceinline__ void fc_continuation(const Geo &g, C2<T> *X, int TK) {
+    // X holds rows [0, nzp) of TK columns; fill rows [nzp, nz)
+    const int C = g.cz, d = g.oz, n = g.nz;
+    for (int idx = threadIdx.x; idx < C * TK; idx += blockDim.x) {
+        const int ii = idx / TK, c = idx % TK;
+        const C2<T> t0 = X[(n - C - d) * TK + c], b0 = X[(d - 1) * TK + c];
+        const double a0 = __ldg(g.dir + ii), a1 = __ldg(g.dir + (C - 1 - ii));
+        double ar = a0 * (double)t0.x + a1 * (double)b0.x;
+        double ai = a0 * (double)t0.y + a1 * (double)b0.y;
+        for (int jj = 1; jj < d; jj++) {
+            const C2<T> t = X[(n - C - d + jj) * TK + c], b = X[(d - 1 - jj) * TK + c];
+            const double w0 = __ldg(g.dir + ii + C * jj), w1 = __ldg(g.dir + (C - 1 - ii) + C * jj);
+            ar = ar + w0 * (double)t.x + w1 * (double)b.x;
+            ai = ai + w0 * (double)t.y + w1 * (double)b.y;
+        }
+        X[(n - C + ii) * TK + c] = mk<T>((T)ar, (T)ai);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_z_forward(Geo g, FFTDesc fd, ZFwdArgs a, int TK) {
+    using V = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * TK;
+    const int kx0 = blockIdx.x * TK, ky = blockIdx.y, f = blockIdx.z;
+    const V *in = (const V *)a.in[f];
+    V *out = (V *)a.out[f];
+    const int nv = min(TK, g.nxh - kx0);
+    const T s = (T)a.in_scale;
+    for (int idx = threadIdx.x; idx < g.nzp * TK; idx += blockDim.x) {
+        const int k = idx / TK, c = idx % TK;
+        V v = mk<T>(0, 0);
+        if (c < nv) v = in[fidx<T>(g, k, ky, kx0 + c)];
+        X[idx] = a.in_scale != 1.0 ? cscale(v, s) : v;
+    }
+    __syncthreads();
+    fc_continuation<T>(g, X, TK);
+    __syncthreads();
+    V *R = fft_exec<T>(X, Y, TK, fd, -1);
+    for (int idx = threadIdx.x; idx < g.nz * TK; idx += blockDim.x) {
+        const int k = idx / TK, c = idx % TK;
+        if (c < nv) out[fidx<T>(g, k, ky, kx0 + c)] = R[idx];
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// y pass: out0 = scale * FFT_y^sign(in), out1 = scale * FFT_y^sign(i ky in), planes [0, nplanes).
+// ---------------------------------------------------------------------------------
+struct YArgs {
+    const void *in[kMaxF];
+    void *out0[kMaxF];
+    void *out1[kMaxF];
+    int sign;
+    double scale;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_y_pass(Geo g, FFTDesc fd, YArgs a, int TK) {
+    using V = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * TK;
+    const int kx0 = blockIdx.x * TK, z = blockIdx.y, f = blockIdx.z;
+    const V *in = (const V *)a.in[f];
+    const int nv = min(TK, g.nxh - kx0);
+    for (int pass = 1; pass >= 0; pass--) {  // derivative output first: out0 may alias in
+        V *out = (V *)(pass == 0 ? a.out0[f] : a.out1[f]);
+        if (!out) continue;
+        for (int idx = threadIdx.x; idx < g.ny * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            V v = mk<T>(0, 0);
+            if (c < nv) v = in[fidx<T>(g, z, k, kx0 + c)];
+            if (pass == 1) v = cimk((T)g.ky[k], v);
+            X[idx] = v;
+        }
+        __syncthreads();
+        V *R = fft_exec<T>(X, Y, TK, fd, a.sign);
+        for (int idx = threadIdx.x; idx < g.ny * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            if (c < nv) {
+                V v = R[idx];
+                if (a.scale != 1.0) v = cscale(v, (T)a.scale);
+                out[fidx<T>(g, z, k, kx0 + c)] = v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// x pass helpers: real rows of length nx = 2H through a complex FFT of length H.
+// ---------------------------------------------------------------------------------
+
+// Build Z (H rows) for a C2R from the half spectrum S (nxh rows, RB columns):
+// Z_k = (X_k + conj X_{H-k}) + i e^{+2 pi i k/nx} (X_k - conj X_{H-k}); Im X_0 = Im X_H = 0.
+template <typename T>
+__device__ __forceinline__ void c2r_pre(const Geo &g, const C2<T> *S, C2<T> *Z, int RB) {
+    using V = C2<T>;
+    const V *xtw = (const V *)g.xtw;
+    const int H = g.H;
+    for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
+        const int k = idx / RB, r = idx % RB;
+        V xk = S[k * RB + r], xm = S[(H - k) * RB + r];
+        if (k == 0) { xk.y = 0; xm.y = 0; }
+        const V xmc = cconj(xm);
+        const V e = cadd(xk, xmc);
+        V w = __ldg(xtw + k);
+        w.y = -w.y;  // exp(+2 pi i k / nx)
+        const V o = cmul(csub(xk, xmc), w);
+        Z[idx] = mk<T>(e.x - o.y, e.y + o.x);
+    }
+}
+
+// From Z = FFT_H(packed real row), write the half spectrum X_0..X_H (scaled) into S:
+// X_k = (Z_k + conj Z_{H-k})/2 - (i/2) e^{-2 pi i k/nx} (Z_k - conj Z_{H-k}).
+template <typename T>
+__device__ __forceinline__ void r2c_post(const Geo &g, const C2<T> *Z, C2<T> *S, int RB) {
+    using V = C2<T>;
+    const V *xtw = (const V *)g.xtw;
+    const int H = g.H;
+    for (int idx = threadIdx.x; idx < (H + 1) * RB; idx += blockDim.x) {
+        const int k = idx / RB, r = idx % RB;
+        const V zk = Z[(k % H) * RB + r], zm = cconj(Z[((H - k) % H) * RB + r]);
+        const V e = cadd(zk, zm), d = csub(zk, zm);
+        const V t = cmul(d, __ldg(xtw + k));
+        S[idx] = mk<T>((T)0.5 * (e.x + t.y), (T)0.5 * (e.y - t.x));
+    }
+}
+
+// x pass R2C of real rows: out[row] = FFT_x(r[row]) for rows (z,y), z < nrows.
+struct XArgs {
+    const void *in[kMaxF];
+    void *out[kMaxF];
+    int nrows;  // z planes
+    double scale;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_x_r2c(Geo g, FFTDesc fd, XArgs a, int RB) {
+    using V = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * RB, *S = Y + (size_t)fd.L * RB;
+    const int f = blockIdx.z;
+    const int row0 = blockIdx.x * RB, nrows = a.nrows * g.ny;
+    const T *in = (const T *)a.in[f];
+    V *out = (V *)a.out[f];
+    const int H = g.H;
+    for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
+        const int m = idx / RB, r = idx % RB;
+        V v = mk<T>(0, 0);
+        if (row0 + r < nrows) {
+            const T *p = in + (size_t)(row0 + r) * g.nx + 2 * m;
+            v = mk<T>(p[0], p[1]);
+        }
+        X[idx] = v;
+    }
+    __syncthreads();
+    V *R = fft_exec<T>(X, Y, RB, fd, -1);
+    r2c_post<T>(g, R, S, RB);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < g.nxh * RB; idx += blockDim.x) {
+        const int r = idx / g.nxh, k = idx % g.nxh;
+        if (row0 + r < nrows) {
+            V v = S[k * RB + r];
+            if (a.scale != 1.0) v = cscale(v, (T)a.scale);
+            out[(size_t)(row0 + r) * g.ldx + k] = v;
+        }
+    }
+}
+
+// x pass C2R: r[row] = IFFT_x(in[row]) (Hermitian half spectrum; Im of kx=0, nx/2 ignored)
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_x_c2r(Geo g, FFTDesc fd, XArgs a, int RB) {
+    using V = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * RB, *S = Y + (size_t)fd.L * RB;
+    const int f = blockIdx.z;
+    const int row0 = blockIdx.x * RB, nrows = a.nrows * g.ny;
+    const V *in = (const V *)a.in[f];
+    T *out = (T *)a.out[f];
+    for (int idx = threadIdx.x; idx < g.nxh * RB; idx += blockDim.x) {
+        const int r = idx / g.nxh, k = idx % g.nxh;
+        V v = mk<T>(0, 0);
+        if (row0 + r < nrows) v = in[(size_t)(row0 + r) * g.ldx + k];
+        S[k * RB + r] = v;
+    }
+    __syncthreads();
+    c2r_pre<T>(g, S, X, RB);
+    __syncthreads();
+    V *R = fft_exec<T>(X, Y, RB, fd, +1);
+    const int H = g.H;
+    for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
+        const int r = idx / H, m = idx % H;
+        if (row0 + r < nrows) {
+            V v = R[m * RB + r];
+            if (a.scale != 1.0) v = cscale(v, (T)a.scale);
+            T *p = out + (size_t)(row0 + r) * g.nx + 2 * m;
+            p[0] = v.x;
+            p[1] = v.y;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Fused x pass for the nonlinear terms (gradre, pseudospec_hd.f90:209-319, and advect,
+// pseudospec_phd.f90:23-113).  Per (y,z) row, inputs are the y-inverse-transformed rows
+// U_j (velocity), DY_i = d/dy v_i, DZ_i = d/dz v_i (and TH, DYT, DZT for the scalar).
+// d/dx is i*kx applied to the spectral row.  Physical rows stay packed as H complex
+// numbers (x_{2m} + i x_{2m+1}); products act on real and imaginary parts separately.
+//   NL_i = ((u_x d_x v_i + u_y d_y v_i) + u_z d_z v_i) * 1/(nx ny nz)^2
+// then a forward R2C of each NL_i.
+// ---------------------------------------------------------------------------------
+struct XNLArgs {
+    const void *u[4];    // v_x, v_y, v_z, theta rows (z,y,kx); u[3] only when c1 == 4
+    const void *dy[4];   // d/dy v_x, v_y, v_z, theta
+    const void *dz[4];   // d/dz v_x, v_y, v_z, theta
+    void *out[4];        // NL_x, NL_y, NL_z, NL_theta  (z,y,kx)
+    int c0, c1;          // components [c0, c1) are formed (0..2 velocity, 3 scalar)
+    int nrows;           // physical z planes
+    double tmp;          // 1/(nx ny nz)^2
+};
+
+template <typename T>
+__device__ __forceinline__ void load_row_spec(const Geo &g, const C2<T> *in, C2<T> *S, int row0, int nrows, int RB, int dx) {
+    using V = C2<T>;
+    for (int idx = threadIdx.x; idx < g.nxh * RB; idx += blockDim.x) {
+        const int r = idx / g.nxh, k = idx % g.nxh;
+        V v = mk<T>(0, 0);
+        if (row0 + r < nrows) v = in[(size_t)(row0 + r) * g.ldx + k];
+        if (dx) v = cimk((T)g.kx[k], v);
+        S[k * RB + r] = v;
+    }
+}
+
+// C2R of a spectral row set held in S into P (H x RB packed physical)
+template <typename T>
+__device__ __forceinline__ void c2r_rows(const Geo &g, const FFTDesc &fd, C2<T> *S, C2<T> *X, C2<T> *Y, C2<T> *P, int RB) {
+    __syncthreads();
+    c2r_pre<T>(g, S, X, RB);
+    __syncthreads();
+    C2<T> *R = fft_exec<T>(X, Y, RB, fd, +1);
+    for (int idx = threadIdx.x; idx < g.H * RB; idx += blockDim.x) P[idx] = R[idx];
+    __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_x_nonlinear(Geo g, FFTDesc fd, XNLArgs a, int RB) {
+    using V = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int H = g.H, L = fd.L;
+    V *X = (V *)smem_raw;
+    V *Y = X + (size_t)L * RB;
+    V *S = Y + (size_t)L * RB;                 // nxh * RB spectral row staging
+    V *U = S + (size_t)g.nxh * RB;              // 3 * H * RB physical velocity rows
+    V *P = U + (size_t)3 * H * RB;              // H * RB product operand
+    V *A = P + (size_t)H * RB;                  // (c1-c0) * H * RB accumulators
+    const int c0 = a.c0, c1 = a.c1;
+    const int row0 = blockIdx.x * RB, nrows = a.nrows * g.ny;
+    // velocity rows; after each, the x-derivative term of the same component
+    for (int j = 0; j < 3; j++) {
+        load_row_spec<T>(g, (const V *)a.u[j], S, row0, nrows, RB, 0);
+        c2r_rows<T>(g, fd, S, X, Y, U + (size_t)j * H * RB, RB);
+    }
+    // term 1: u_x * d/dx v_i (and theta)
+    for (int i = c0; i < c1; i++) {
+        load_row_spec<T>(g, (const V *)a.u[i], S, row0, nrows, RB, 1);
+        c2r_rows<T>(g, fd, S, X, Y, P, RB);
+        for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
+            const V u = U[idx], p = P[idx];
+            A[(size_t)(i - c0) * H * RB + idx] = mk<T>(u.x * p.x, u.y * p.y);
+        }
+    }
+    // term 2: + u_y * d/dy v_i
+    for (int i = c0; i < c1; i++) {
+        load_row_spec<T>(g, (const V *)a.dy[i], S, row0, nrows, RB, 0);
+        c2r_rows<T>(g, fd, S, X, Y, P, RB);
+        for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
+            const V u = U[(size_t)H * RB + idx], p = P[idx];
+            V &acc = A[(size_t)(i - c0) * H * RB + idx];
+            acc = mk<T>(acc.x + u.x * p.x, acc.y + u.y * p.y);
+        }
+    }
+    // term 3: (acc + u_z * d/dz v_i) * tmp, then R2C
+    const T tmp = (T)a.tmp;
+    for (int i = c0; i < c1; i++) {
+        load_row_spec<T>(g, (const V *)a.dz[i], S, row0, nrows, RB, 0);
+        c2r_rows<T>(g, fd, S, X, Y, P, RB);
+        for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
+            const V u = U[(size_t)2 * H * RB + idx], p = P[idx];
+            const V acc = A[(size_t)(i - c0) * H * RB + idx];
+            X[idx] = mk<T>((acc.x + u.x * p.x) * tmp, (acc.y + u.y * p.y) * tmp);
+        }
+        __syncthreads();
+        V *R = fft_exec<T>(X, Y, RB, fd, -1);
+        r2c_post<T>(g, R, S, RB);
+        __syncthreads();
+        V *out = (V *)a.out[i];
+        for (int idx = threadIdx.x; idx < g.nxh * RB; idx += blockDim.x) {
+            const int r = idx / g.nxh, k = idx % g.nxh;
+            if (row0 + r < nrows) out[(size_t)(row0 + r) * g.ldx + k] = S[k * RB + r];
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace sg
