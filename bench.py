@@ -1,0 +1,294 @@
+"""Benchmark of SPECTER's per-RK-stage hot path on GB300.
+
+Workload (one "step" = one RK2 step = 2 RK stages over the whole grid): the Boussinesq
+Rayleigh-Benard case, nx = ny = 512 (periodic, Lx = Ly = 2*pi), nz = 513 physical points
+(+ Cz = 25 FC-Gram continuation points, NZ = 538) on z in [0, 1], d = 5, Pr = 1,
+nu = kappa = 1e-4, RK order 2, dt = 1e-5, in the FP32-bulk precision form; seeded synthetic
+initial field (theta' = 1e-3 * U(-1,1) * z(1 - z), v = 0).  Each field is 566 MB, far larger
+than the 129 MB L2, so no L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  `value` is grid points x RK stages per second with the state
+resident in HBM; `e2e` is the same metric through the C ABI with the state uploaded from
+pinned host memory and downloaded back every step.  `--impl reference` times the FP64 CPU
+restatement of the reference algorithm (the oracle; the Fortran reference cannot be built
+here) on a bounded sample of the same workload on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RK-stage Mpts/s FP32-bulk vs FP64 at ≤1e-5 rel err; ensemble solves/s, p99 lat"
+UNIT = "Mpts*stages/s"
+CFG = dict(nx=512, ny=512, nzp=513, cz=25, oz=5, Lx=1.0, Ly=1.0, Lz=1.0,
+           solver="BOUSS", ord=2, dt=1e-5, nu=1e-4, kappa=1e-4, seed=20261203)
+# CPU sample: same z grid and physics, 128 x 128 in (x, y), one RK2 step per timed step
+CPU_SAMPLE = dict(CFG, nx=128, ny=128)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu, self.rows, self.proc = gpu, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def build_solver(api, initial, cfg, precision, fused=True):
+    nz = cfg["nzp"] + cfg["cz"]
+    plan = api.Plan((cfg["nx"], cfg["ny"], nz), (0, 0, cfg["cz"]), (0, 0, cfg["oz"]),
+                    (cfg["Lx"], cfg["Ly"], cfg["Lz"]), precision=precision)
+    s = api.Solver(plan, api.BOUSS, ord=cfg["ord"], dt=cfg["dt"], nu=cfg["nu"], kappa=cfg["kappa"], fused=fused)
+    th = initial.convection_theta(plan, seed=cfg["seed"], amp=1e-3)
+    fth = initial.to_spectral(plan, [th])[0]
+    s.th.copy_from(fth)
+    for f in (s.vx, s.vy, s.vz, s.pr):
+        f.zero()
+    plan.synchronize()
+    return plan, s
+
+
+def dominant_roofline(report, hbm_peak, traffic_table):
+    name, (n, ms, b) = max(report.items(), key=lambda kv: kv[1][1])
+    per_ms = ms / n
+    per_bytes = b / n
+    achieved = per_bytes / (per_ms * 1e-3) / 1e9
+    traffic = traffic_table.get(name)
+    return {"kernel": name, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+            "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
+            "algorithmic_bytes_per_launch": per_bytes, "avg_launch_ms": round(per_ms, 4),
+            "launches": n, "share": round(ms / sum(v[1] for v in report.values()), 4)}
+
+
+def load_traffic():
+    """Per-launch DRAM bytes of each kernel from the committed ncu summary (profiles/)."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic_bouss512.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def cpu_baseline(steps, warmup, threads=None):
+    """The oracle (FP64 CPU restatement) on the bounded sample; returns (value, cores, sample)."""
+    import numpy as np
+    from oracle import oracle as O
+    O.build()
+    threads = threads or os.cpu_count()
+    O.set_threads(threads)
+    c = CPU_SAMPLE
+    g = O.Grid(c["nx"], c["ny"], c["nzp"] + c["cz"], c["cz"], c["oz"], c["Lx"], c["Ly"], c["Lz"])
+    rng = np.random.default_rng(c["seed"])
+    th = np.zeros(g.rshape)
+    z = g.z[: c["nzp"]]
+    th[: c["nzp"]] = 1e-3 * rng.uniform(-1, 1, (c["nzp"], c["ny"], c["nx"])) * (z * (c["Lz"] - z))[:, None, None]
+    tht = g.fftp3d_real_to_complex(th)
+    zero = np.zeros(g.sshape, complex)
+    p = g.params(dt=c["dt"], nu=c["nu"], ord=c["ord"], kappa=c["kappa"])
+    state = (zero, zero, zero, tht, zero)
+    for _ in range(warmup):
+        out = g.run(p, 1, *state[:3], state[4], th=state[3])
+        state = (out[0], out[1], out[2], out[3], out[4])
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        out = g.run(p, 1, *state[:3], state[4], th=state[3])
+        state = (out[0], out[1], out[2], out[3], out[4])
+    dt = time.perf_counter() - t0
+    pts = c["nx"] * c["ny"] * c["nzp"] * c["ord"] * steps
+    sample = (f"{c['nx']}x{c['ny']}x{c['nzp']} (+{c['cz']}) BOUSS RK2, {steps} step(s) of the FP64 oracle, "
+              f"{threads} threads")
+    return pts / dt / 1e6, threads, sample
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement of the reference algorithm on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    steps = max(1, min(args.steps, 3))
+    warmup = 1 if args.warmup > 0 else 0
+    value, cores, sample = cpu_baseline(steps, warmup)
+    line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "impl": "reference",
+            "n_gpus": args.gpus, "steps": steps, "warmup": warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "BOUSS Rayleigh-Benard 512x512x513 (+25 FC-Gram), RK2, dt=1e-5; "
+                                   "timed on the bounded sample", "sample_grid": "128x128x513",
+                       "parallelism": "host threads"},
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--refseq", action="store_true", help="time the reference call sequence instead of the fused stages")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    from specter_gb300 import api, initial
+    api.set_device(local)
+    K, W = args.steps, max(args.warmup, 3)
+
+    plan, s = build_solver(api, initial, CFG, api.FP32, fused=not args.refseq)
+    stream = torch.cuda.ExternalStream(plan.stream, device=torch.device("cuda", local))
+    for _ in range(W):
+        s.step(1)
+    plan.synchronize()
+    if dist:
+        dist.barrier()
+    plan.profile(True)
+    n0 = plan.launch_count
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(K):
+            s.step(1)
+        ev1.record(stream)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    launches = plan.launch_count - n0
+    report = plan.profile_report()
+    plan.profile(False)
+    s.check()
+    t = torch.tensor([ms], device=f"cuda:{local}")
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    pts = CFG["nx"] * CFG["ny"] * CFG["nzp"]
+    value = world * pts * CFG["ord"] * K / (ms * 1e-3) / 1e6
+
+    # end to end: state uploaded from pinned host memory and downloaded every step
+    fields = [f for f in (s.vx, s.vy, s.vz, s.th, s.pr)]
+    host = [torch.empty(f.nbytes, dtype=torch.uint8, pin_memory=True) for f in fields]
+    for f, h in zip(fields, host):
+        f.download_ptr(h.data_ptr())
+    Ke = max(2, K // 2)
+    plan.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        for f, h in zip(fields, host):
+            f.upload_ptr(h.data_ptr())
+        s.step(1)
+        for f, h in zip(fields, host):
+            f.download_ptr(h.data_ptr())
+    plan.synchronize()
+    te = time.perf_counter() - t0
+    te_t = torch.tensor([te], device=f"cuda:{local}")
+    if dist:
+        dist.all_reduce(te_t, op=dist.ReduceOp.MAX)
+    e2e = world * pts * CFG["ord"] * Ke / float(te_t.item()) / 1e6
+    nbytes = sum(f.nbytes for f in fields)
+
+    if rank == 0:
+        peak, peak_kind = peaks()
+        roof = dominant_roofline(report, peak, load_traffic())
+        roof["peak_kind"] = peak_kind
+        # stage-level model of the frozen measurement definition: B = 128 * N * s per BOUSS stage
+        N = CFG["nx"] * CFG["ny"] * (CFG["nzp"] + CFG["cz"])
+        model_gbs = 128 * N * 4 * CFG["ord"] * K / (ms * 1e-3) / 1e9
+        line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": K,
+                "warmup": W, "ms_per_step": round(ms / K, 4), "higher_is_better": True,
+                "scaling": "weak" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic",
+                "config": {"workload": "BOUSS Rayleigh-Benard 512x512x513 (+25 FC-Gram, NZ=538), FP32-bulk, RK2, dt=1e-5",
+                           "path": "reference-sequence" if args.refseq else "fused",
+                           "l2": "inputs larger than L2 (566 MB per field), no flush",
+                           "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+                "roofline": roof,
+                "stage_model": {"bytes_per_stage": 128 * N * 4, "achieved_gbs": round(model_gbs, 1),
+                                "frac": round(model_gbs / peak, 4)},
+                "kernels": {k: {"launches": v[0], "ms": round(v[1], 3),
+                                "gbs": round(v[2] / (v[1] * 1e-3) / 1e9, 1) if v[1] > 0 else None}
+                            for k, v in sorted(report.items(), key=lambda kv: -kv[1][1])},
+                "clocks": clocks.summary(),
+                "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
+                "gpu_launches": launches}
+        if not args.no_cpu and world == 1:
+            v, cores, sample = cpu_baseline(1, 0)
+            line["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -47,6 +47,8 @@ typedef struct specter_solver specter_solver;
 const char *specter_last_error(void);
 int specter_version(void);
 int specter_device_count(int *count);
+/* selects the CUDA device used by plans created afterwards on the calling thread */
+int specter_set_device(int device);
 
 /* ---- plan: fcgram_create_plan (src/fftp/fcgram_mod.f90:49-144) + grid/kes setup
  *      (src/specter.fpp:683-800).  n = (nx, ny, nz) totals, c = (Cx, Cy, Cz), o = (ox, oy, oz)
@@ -141,6 +143,15 @@ int specter_solver_check(specter_solver *s);
  *      accumulated from CUDA events (the reference's fftp_mod.fpp:32-37 accumulators) */
 int specter_timers(specter_plan *plan, double out[6]);
 int specter_timers_reset(specter_plan *plan);
+
+/* ---- kernel accounting (no reference counterpart; measurement support).
+ *      specter_profile(plan, 1) brackets every kernel launch of the plan with CUDA events on
+ *      the plan stream; specter_profile_report writes one line per kernel name:
+ *      "name launches total_ms algorithmic_bytes\n" (reset with specter_profile(plan, 0)).
+ *      specter_launch_count returns the number of kernels the plan has launched. */
+int specter_profile(specter_plan *plan, int enable);
+int specter_profile_report(specter_plan *plan, char *buf, int buflen);
+int specter_launch_count(specter_plan *plan, long long *count);
 
 #ifdef __cplusplus
 }

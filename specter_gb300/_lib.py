@@ -16,7 +16,7 @@ ERR_NAMES = {1: "SHAPE", 2: "TABLE", 3: "BC", 4: "OOM", 5: "CUDA", 6: "NONFINITE
 
 # every entry point declared in include/specter_gpu.h
 EXPORTS = [
-    "specter_last_error", "specter_version", "specter_device_count",
+    "specter_last_error", "specter_version", "specter_device_count", "specter_set_device",
     "specter_plan_create", "specter_plan_destroy", "specter_plan_info", "specter_plan_arrays",
     "specter_plan_synchronize", "specter_plan_stream",
     "specter_field_create", "specter_field_destroy", "specter_field_upload", "specter_field_download",
@@ -31,6 +31,7 @@ EXPORTS = [
     "specter_solver_create", "specter_solver_destroy", "specter_solver_fields", "specter_solver_step",
     "specter_solver_stage", "specter_solver_check",
     "specter_timers", "specter_timers_reset",
+    "specter_profile", "specter_profile_report", "specter_launch_count",
 ]
 
 

@@ -26,6 +26,11 @@ def _pd(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def set_device(device: int) -> None:
+    """CUDA device for plans created afterwards on this thread."""
+    check(load().specter_set_device(int(device)))
+
+
 class Plan:
     """fcgram_create_plan (src/fftp/fcgram_mod.f90:49-144) plus the grid / kes setup
     (src/specter.fpp:683-800).  n = (nx, ny, nz) with nz the total z size (physical + Cz)."""
@@ -92,6 +97,26 @@ class Plan:
         check(self._L.specter_timers(self.h, out))
         return list(out)
 
+    def profile(self, enable=True):
+        """Bracket every kernel launch with CUDA events (resets the per-kernel report)."""
+        check(self._L.specter_profile(self.h, 1 if enable else 0))
+
+    def profile_report(self):
+        """{kernel: (launches, total_ms, algorithmic_bytes)} since profiling was enabled."""
+        buf = C.create_string_buffer(1 << 16)
+        check(self._L.specter_profile_report(self.h, buf, len(buf)))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, n, ms, b = line.split()
+            out[name] = (int(n), float(ms), float(b))
+        return out
+
+    @property
+    def launch_count(self) -> int:
+        n = C.c_longlong()
+        check(self._L.specter_launch_count(self.h, C.byref(n)))
+        return n.value
+
 
 class Field:
     """Device-resident field handle (complex spectral/mixed or real physical)."""
@@ -128,6 +153,19 @@ class Field:
     @property
     def dtype(self):
         return self.plan.cdtype if self.kind == COMPLEX else self.plan.rdtype
+
+    @property
+    def nbytes(self) -> int:
+        """Bytes of the host array in the reference layout."""
+        return int(np.prod(self.shape)) * np.dtype(self.dtype).itemsize
+
+    def upload_ptr(self, host_ptr: int):
+        """Asynchronous upload from a host buffer (reference layout) at host_ptr."""
+        check(self.plan._L.specter_field_upload(self.h, C.c_void_p(host_ptr)))
+
+    def download_ptr(self, host_ptr: int):
+        """Download into a host buffer (reference layout); returns when the data is there."""
+        check(self.plan._L.specter_field_download(self.h, C.c_void_p(host_ptr)))
 
     def upload(self, a):
         a = np.ascontiguousarray(a, dtype=self.dtype)

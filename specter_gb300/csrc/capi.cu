@@ -69,6 +69,12 @@ extern "C" {
 const char *specter_last_error(void) { return sg::last_error(); }
 int specter_version(void) { return 100; }
 
+int specter_set_device(int device) {
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return SPECTER_ERR_CUDA; }
+    return SPECTER_OK;
+}
+
 int specter_device_count(int *count) {
     int n = 0;
     cudaError_t e = cudaGetDeviceCount(&n);
@@ -201,6 +207,8 @@ static int staging(Plan &P, void **buf) {
 
 static int convert(Plan &P, const void *src, void *dst, bool to_dev) {
     dim3 grid(cdiv(P.nz, 32), cdiv(P.nxh, 32), P.ny), block(32, 8);
+    P.prof_begin(to_dev ? "layout_to_device" : "layout_to_reference", 2.0 * P.nz * P.ny * P.nxh * P.elt());
+    struct End { Plan &P; ~End() { P.prof_end(); } } end{P};
     if (P.prec == FP64) {
         if (to_dev) k_ref_to_dev<double2><<<grid, block, 0, P.stream>>>((const double2 *)src, (double2 *)dst, P.nz, P.ny, P.nxh, P.ldx);
         else k_dev_to_ref<double2><<<grid, block, 0, P.stream>>>((const double2 *)src, (double2 *)dst, P.nz, P.ny, P.nxh, P.ldx);
@@ -472,6 +480,14 @@ int specter_solver_step(specter_solver *s, int nsteps) {
     if (!s) { set_error("null solver"); return SPECTER_ERR_ARG; }
     Plan &P = *s->plan->p;
     const int nc = s->sp.solver == SPECTER_BOUSS ? 4 : 3;
+    if (s->fused) {
+        void *v[4] = {s->v[0]->d, s->v[1]->d, s->v[2]->d, s->v[3] ? s->v[3]->d : nullptr};
+        for (int t = 0; t < nsteps; t++) {
+            int st = fused_step(P, s->fs, v, s->pr->d);
+            if (st) return st;
+        }
+        return SPECTER_OK;
+    }
     for (int t = 0; t < nsteps; t++) {
         // rkstep1: C_i = v_i (hd_rkstep1.f90:4-6, bouss_rkstep1.f90:4-7)
         for (int i = 0; i < nc; i++)
@@ -508,6 +524,36 @@ int specter_timers(specter_plan *plan, double out[6]) {
 int specter_timers_reset(specter_plan *plan) {
     CHECK_PLAN(plan);
     for (int i = 0; i < 6; i++) plan->p->timers[i] = 0.0;
+    return SPECTER_OK;
+}
+
+int specter_profile(specter_plan *plan, int enable) {
+    CHECK_PLAN(plan);
+    Plan &P = *plan->p;
+    P.prof_flush();
+    P.agg.clear();
+    P.profile = enable != 0;
+    return SPECTER_OK;
+}
+
+int specter_profile_report(specter_plan *plan, char *buf, int buflen) {
+    CHECK_PLAN(plan);
+    Plan &P = *plan->p;
+    P.prof_flush();
+    std::string out;
+    char line[256];
+    for (const Plan::Agg &g : P.agg) {
+        snprintf(line, sizeof line, "%s %lld %.6f %.0f\n", g.name.c_str(), g.n, g.ms, g.bytes);
+        out += line;
+    }
+    if (!buf || buflen <= (int)out.size()) { set_error("report buffer too small"); return SPECTER_ERR_ARG; }
+    memcpy(buf, out.c_str(), out.size() + 1);
+    return SPECTER_OK;
+}
+
+int specter_launch_count(specter_plan *plan, long long *count) {
+    CHECK_PLAN(plan);
+    *count = plan->p->launches;
     return SPECTER_OK;
 }
 

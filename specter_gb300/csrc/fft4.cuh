@@ -1,0 +1,251 @@
+// Register-resident four-step FFT over shared-memory column tiles (device side).
+//
+// A length L = L1*L2 transform of B columns held in smem at X[pos*B + col] runs in two
+// exchange steps instead of one smem round trip per radix stage:
+//   step A  thread (col, n2): loads x[n2 + L2*n1], n1 < L1, does DFT_L1 in registers,
+//           multiplies by w_L^{n2*k1}, stores back to the same positions n2 + L2*k1;
+//   step B  thread (col, k1): loads the contiguous run L2*k1 + n2, n2 < L2, does DFT_L2 in
+//           registers and stores frequency k1 + L1*k2 at position L2*k1 + k2 ("permuted").
+// The inverse-order pair (B' then A') takes permuted input to natural output.  Bluestein's
+// algorithm fuses as  A (input * chirp) | B, *filter, B' (all in registers) | A' (* chirp):
+// two barriers and two smem round trips for a convolution of length L.
+//
+// Register DFTs are unrolled mixed-radix Stockham sequences with compile-time radices; their
+// internal twiddles come from a __constant__ table (uniform address -> constant-bank operand).
+// Both tables are filled per translation unit by fft4_init_tables().
+#pragma once
+
+#include "common.cuh"
+#include "fft.cuh"
+#include "plan.h"
+
+namespace sg {
+
+// ---- register DFT sizes served by the constant twiddle table -------------------------------
+constexpr int kRegSizes[] = {8, 9, 10, 12, 15, 16, 18, 20, 24, 27, 30, 32, 36, 40, 45, 48, 64};
+constexpr int kNumRegSizes = sizeof(kRegSizes) / sizeof(int);
+constexpr int reg_offset(int N) {
+    int off = 0;
+    for (int i = 0; i < kNumRegSizes; i++) {
+        if (kRegSizes[i] == N) return off;
+        off += kRegSizes[i];
+    }
+    return -1;
+}
+constexpr int kRegTableLen = reg_offset(64) + 64;
+
+constexpr int pick_radix(int m) {
+    return m % 4 == 0 ? 4 : m % 2 == 0 ? 2 : m % 3 == 0 ? 3 : m % 5 == 0 ? 5 : m;
+}
+
+// per translation unit: w_N^t = exp(-2 pi i t / N) for every N in kRegSizes
+static __constant__ float2 c_regtw_f[kRegTableLen];
+static __constant__ double2 c_regtw_d[kRegTableLen];
+
+template <typename T> __device__ __forceinline__ C2<T> regtw(int i);
+template <> __device__ __forceinline__ float2 regtw<float>(int i) { return c_regtw_f[i]; }
+template <> __device__ __forceinline__ double2 regtw<double>(int i) { return c_regtw_d[i]; }
+
+// upload the constant tables of this translation unit (host)
+static inline cudaError_t fft4_init_tables() {
+    static float2 hf[kRegTableLen];
+    static double2 hd[kRegTableLen];
+    const long double pi = 3.14159265358979323846264338327950288L;
+    for (int i = 0; i < kNumRegSizes; i++) {
+        const int N = kRegSizes[i], off = reg_offset(N);
+        for (int t = 0; t < N; t++) {
+            long double a = -2.0L * pi * t / N;
+            hd[off + t] = make_double2((double)cosl(a), (double)sinl(a));
+            hf[off + t] = make_float2((float)cosl(a), (float)sinl(a));
+        }
+    }
+    cudaError_t e = cudaMemcpyToSymbol(c_regtw_f, hf, sizeof hf);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_regtw_d, hd, sizeof hd);
+    return e;
+}
+
+// The tables are per translation unit: every TU that launches four-step kernels calls this
+// before its launches (uploads once per device).
+static inline cudaError_t fft4_ensure_tables() {
+    static bool done[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+    cudaError_t e = fft4_init_tables();
+    if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
+    return e;
+}
+
+// one register Stockham stage chain: a holds the data, b is scratch; result ends in `a`
+template <typename T, int N, int SIGN, int Ns>
+struct RegStages {
+    static __device__ __forceinline__ void run(C2<T> *a, C2<T> *b) {
+        if constexpr (Ns < N) {
+            constexpr int R = pick_radix(N / Ns);
+            constexpr int nR = N / R;
+            constexpr int step = N / (Ns * R);
+            constexpr int off = reg_offset(N);
+#pragma unroll
+            for (int j = 0; j < nR; j++) {
+                const int k = j % Ns;
+                C2<T> t[R];
+#pragma unroll
+                for (int q = 0; q < R; q++) {
+                    t[q] = a[j + q * nR];
+                    if (q && k) {
+                        C2<T> w = regtw<T>(off + q * k * step);
+                        if (SIGN > 0) w.y = -w.y;
+                        t[q] = cmul(t[q], w);
+                    }
+                }
+                butterfly<T, R>(t, SIGN, nullptr, 0);
+                const int base = (j / Ns) * Ns * R + k;
+#pragma unroll
+                for (int q = 0; q < R; q++) b[base + q * Ns] = t[q];
+            }
+#pragma unroll
+            for (int i = 0; i < N; i++) a[i] = b[i];
+            RegStages<T, N, SIGN, Ns * R>::run(a, b);
+        }
+    }
+};
+
+template <typename T, int N, int SIGN>
+__device__ __forceinline__ void dft_reg(C2<T> (&a)[N]) {
+    static_assert(reg_offset(N) >= 0, "register DFT size not in the constant table");
+    C2<T> b[N];
+    RegStages<T, N, SIGN, 1>::run(a, b);
+}
+
+// twiddle w_L^{SIGN * t} from a global table tw[t] = exp(-2 pi i t / L)
+template <typename T, int SIGN>
+__device__ __forceinline__ C2<T> gtw(const C2<T> *tw, int t) {
+    C2<T> w = __ldg(tw + t);
+    if (SIGN > 0) w.y = -w.y;
+    return w;
+}
+
+// Four-step tables of one length (FFT4Desc, plan.h), in global memory per plan:
+//   tw4[n2*L1 + k1] = w_L^{n2*k1}               (inter-step twiddles)
+//   chirp[k]        = exp(-i pi k^2 / n), k < n   (Bluestein only)
+//   filtf/filtb[k1*L2 + k2] = filter at frequency k1 + L1*k2, times 1/L (Bluestein only)
+
+// ---- natural -> permuted (steps A, B) ---------------------------------------------------------
+template <typename T, int L1, int L2, int SIGN>
+__device__ __forceinline__ void fft4_np(C2<T> *X, int B, const FFT4Desc &d) {
+    constexpr int L = L1 * L2;
+    const C2<T> *tw4 = (const C2<T> *)d.tw4;
+    for (int idx = threadIdx.x; idx < B * L2; idx += blockDim.x) {
+        const int c = idx % B, n2 = idx / B;
+        C2<T> a[L1];
+#pragma unroll
+        for (int n1 = 0; n1 < L1; n1++) a[n1] = X[(n2 + L2 * n1) * B + c];
+        dft_reg<T, L1, SIGN>(a);
+#pragma unroll
+        for (int k1 = 1; k1 < L1; k1++) a[k1] = cmul(a[k1], gtw<T, SIGN>(tw4, n2 * L1 + k1));
+#pragma unroll
+        for (int k1 = 0; k1 < L1; k1++) X[(n2 + L2 * k1) * B + c] = a[k1];
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < B * L1; idx += blockDim.x) {
+        const int c = idx % B, k1 = idx / B;
+        C2<T> b[L2];
+#pragma unroll
+        for (int n2 = 0; n2 < L2; n2++) b[n2] = X[(L2 * k1 + n2) * B + c];
+        dft_reg<T, L2, SIGN>(b);
+#pragma unroll
+        for (int k2 = 0; k2 < L2; k2++) X[(L2 * k1 + k2) * B + c] = b[k2];
+    }
+    __syncthreads();
+    (void)L;
+}
+
+// ---- permuted -> natural (steps B', A') -------------------------------------------------------
+template <typename T, int L1, int L2, int SIGN>
+__device__ __forceinline__ void fft4_pn(C2<T> *X, int B, const FFT4Desc &d) {
+    const C2<T> *tw4 = (const C2<T> *)d.tw4;
+    for (int idx = threadIdx.x; idx < B * L1; idx += blockDim.x) {
+        const int c = idx % B, k1 = idx / B;
+        C2<T> b[L2];
+#pragma unroll
+        for (int k2 = 0; k2 < L2; k2++) b[k2] = X[(L2 * k1 + k2) * B + c];
+        dft_reg<T, L2, SIGN>(b);
+#pragma unroll
+        for (int m2 = 1; m2 < L2; m2++) b[m2] = cmul(b[m2], gtw<T, SIGN>(tw4, m2 * L1 + k1));
+#pragma unroll
+        for (int m2 = 0; m2 < L2; m2++) X[(L2 * k1 + m2) * B + c] = b[m2];
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < B * L2; idx += blockDim.x) {
+        const int c = idx % B, m2 = idx / B;
+        C2<T> a[L1];
+#pragma unroll
+        for (int k1 = 0; k1 < L1; k1++) a[k1] = X[(L2 * k1 + m2) * B + c];
+        dft_reg<T, L1, SIGN>(a);
+#pragma unroll
+        for (int m1 = 0; m1 < L1; m1++) X[(m2 + L2 * m1) * B + c] = a[m1];
+    }
+    __syncthreads();
+}
+
+// position in the permuted layout of frequency k
+template <int L1, int L2>
+__device__ __forceinline__ int perm_pos(int k) { return L2 * (k % L1) + k / L1; }
+
+// ---- Bluestein over L = L1*L2: natural rows [0, n) in, natural rows [0, n) out (SIGN) ------------
+// Rows [n, L) of X are zeroed here; the caller fills rows [0, n) and syncs first.
+template <typename T, int L1, int L2, int SIGN>
+__device__ __forceinline__ void fft4_bluestein(C2<T> *X, int B, const FFT4Desc &d) {
+    const C2<T> *tw4 = (const C2<T> *)d.tw4;
+    const C2<T> *chirp = (const C2<T> *)d.chirp;
+    const C2<T> *filt = (const C2<T> *)(SIGN < 0 ? d.filtf : d.filtb);
+    const int n = d.n;
+    // step A (forward): input * chirp_SIGN
+    for (int idx = threadIdx.x; idx < B * L2; idx += blockDim.x) {
+        const int c = idx % B, n2 = idx / B;
+        C2<T> a[L1];
+#pragma unroll
+        for (int n1 = 0; n1 < L1; n1++) {
+            const int pos = n2 + L2 * n1;
+            a[n1] = pos < n ? cmul(X[pos * B + c], gtw<T, SIGN>(chirp, pos)) : mk<T>(0, 0);
+        }
+        dft_reg<T, L1, -1>(a);
+#pragma unroll
+        for (int k1 = 1; k1 < L1; k1++) a[k1] = cmul(a[k1], gtw<T, -1>(tw4, n2 * L1 + k1));
+#pragma unroll
+        for (int k1 = 0; k1 < L1; k1++) X[(n2 + L2 * k1) * B + c] = a[k1];
+    }
+    __syncthreads();
+    // step B (forward), filter, step B' (inverse): all in registers
+    for (int idx = threadIdx.x; idx < B * L1; idx += blockDim.x) {
+        const int c = idx % B, k1 = idx / B;
+        C2<T> b[L2];
+#pragma unroll
+        for (int n2 = 0; n2 < L2; n2++) b[n2] = X[(L2 * k1 + n2) * B + c];
+        dft_reg<T, L2, -1>(b);
+#pragma unroll
+        for (int k2 = 0; k2 < L2; k2++) b[k2] = cmul(b[k2], __ldg(filt + k1 * L2 + k2));
+        dft_reg<T, L2, +1>(b);
+#pragma unroll
+        for (int m2 = 1; m2 < L2; m2++) b[m2] = cmul(b[m2], gtw<T, +1>(tw4, m2 * L1 + k1));
+#pragma unroll
+        for (int m2 = 0; m2 < L2; m2++) X[(L2 * k1 + m2) * B + c] = b[m2];
+    }
+    __syncthreads();
+    // step A' (inverse), output * chirp_SIGN on rows < n
+    for (int idx = threadIdx.x; idx < B * L2; idx += blockDim.x) {
+        const int c = idx % B, m2 = idx / B;
+        C2<T> a[L1];
+#pragma unroll
+        for (int k1 = 0; k1 < L1; k1++) a[k1] = X[(L2 * k1 + m2) * B + c];
+        dft_reg<T, L1, +1>(a);
+#pragma unroll
+        for (int m1 = 0; m1 < L1; m1++) {
+            const int pos = m2 + L2 * m1;
+            if (pos < n) X[pos * B + c] = cmul(a[m1], gtw<T, SIGN>(chirp, pos));
+        }
+    }
+    __syncthreads();
+}
+
+}  // namespace sg

@@ -1,0 +1,414 @@
+// Fused RK-stage column kernels.
+//
+// After the nonlinear terms NL_c = (v.grad)v_c (and v.grad theta) have been brought back to
+// the mixed (z, ky, kx) domain by the x/y passes, everything left in a stage acts on single
+// (kx, ky) z-columns.  One block keeps a tile of TK columns resident in shared memory and runs,
+// without touching HBM in between:
+//   velocity:  NL forward z-transform with FC-Gram continuation, buoyancy, fc_filter, laplak and
+//              the RK update (hd_rkstep2.f90:1-32 / bouss_rkstep2.f90:1-48), then
+//              v_imposebc_and_project (vboundary.f90:67-151): z-inverse, no-slip wall planes
+//              from the previous stage's pressure, z-forward with continuation, and sol_project
+//              (boundary_mod.fpp:197-402): Poisson, wall values, laplace_z coefficients (FP64),
+//              pressure, harmonic correction (profiles continued in FP64, then transformed).
+//   scalar:    NL forward, heat current, filter, update, s_imposebc (sboundary.f90:67-165),
+//              fc_filter and the c2r -> /N -> r2c round trip (bouss_rkstep2.f90:56-59).  That
+//              round trip is, exactly, z-inverse, 1/nz, Hermitian symmetrisation of the kx = 0
+//              and kx = nx/2 columns over (ky, -ky) (what C2R then R2C does to them), and
+//              z-forward with continuation; the symmetrisation pairs columns of different
+//              ky, so those two kx columns finish in k_theta_herm.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace sg {
+
+struct FusedArgs {
+    const void *nl[4];    // NL_x, NL_y, NL_z, NL_theta: mixed domain, rows [0, nzp)
+    const void *vin[4];   // stage input state (spectral): vx, vy, vz, theta
+    const void *cold[4];  // RK step start C1, C2, C3, C7
+    void *vout[4];        // stage output state
+    void *pr;             // pressure potential (mixed), walls read, rows [0, nzp) written
+    void *side;           // theta rows of the kx = 0 and kx = nx/2 columns: [2][ny][nzp]
+    double dt, nu, kappa, rmp, xmom, xtemp;
+    double wall_tmp;      // 1/o, or (o+1)/o when o != ord (noslip_z)
+    double vb[4];         // vxzsta, vyzsta, vxzend, vyzend
+    int bouss;
+};
+
+// FC-Gram continuation of rows [nzp, nz) from FP64 values of the first and last d rows.
+// lo(c, j) = row j, hi(c, j) = row nzp - d + j, j < d.
+template <typename T, class LO, class HI>
+__device__ __forceinline__ void fc_continuation_fn(const Geo &g, C2<T> *X, int TK, LO lo, HI hi) {
+    const int C = g.cz, d = g.oz, n = g.nz;
+    for (int idx = threadIdx.x; idx < C * TK; idx += blockDim.x) {
+        const int ii = idx / TK, c = idx % TK;
+        double2 t0 = hi(c, 0), b0 = lo(c, d - 1);
+        const double a0 = __ldg(g.dir + ii), a1 = __ldg(g.dir + (C - 1 - ii));
+        double ar = a0 * t0.x + a1 * b0.x, ai = a0 * t0.y + a1 * b0.y;
+        for (int jj = 1; jj < d; jj++) {
+            const double2 t = hi(c, jj), b = lo(c, d - 1 - jj);
+            const double w0 = __ldg(g.dir + ii + C * jj), w1 = __ldg(g.dir + (C - 1 - ii) + C * jj);
+            ar = ar + w0 * t.x + w1 * b.x;
+            ai = ai + w0 * t.y + w1 * b.y;
+        }
+        X[(n - C + ii) * TK + c] = mk<T>((T)ar, (T)ai);
+    }
+}
+
+// laplace_z profile of column (kx, ky) at grid point zz (boundary_mod.fpp:635-675): a and b = da/dz.
+// EXP = double evaluates the exponentials in FP64; EXP = float in FP32 (the bulk rows of the
+// FP32 form, which are rounded to FP32 for the transform anyway).  Coefficients are FP64.
+template <typename EXP>
+__device__ __forceinline__ void lap_profile(const Geo &g, int kx, int ky, double2 c1, double2 c2, double zz,
+                                            double2 &a, double2 &b) {
+    if (kx == 0 && ky == 0) {
+        a = make_double2(c1.x * zz + c2.x, 0.0);
+        b = make_double2(c1.x, 0.0);
+    } else {
+        const double kh = sqrt(g.kx[kx] * g.kx[kx] + g.ky[ky] * g.ky[ky]);
+        double e1, e2;
+        if constexpr (sizeof(EXP) == 8) { e1 = exp(kh * (zz - g.Lz)); e2 = exp(-(kh * zz)); }
+        else { e1 = (double)expf((float)(kh * (zz - g.Lz))); e2 = (double)expf((float)(-(kh * zz))); }
+        a = make_double2(c1.x * e1 + c2.x * e2, c1.y * e1 + c2.y * e2);
+        b = make_double2(kh * (c1.x * e1 - c2.x * e2), kh * (c1.y * e1 - c2.y * e2));
+    }
+}
+
+// Neumann laplace_z coefficients from the wall values (boundary_mod.fpp:521-549), FP64
+__device__ __forceinline__ void lap_coef_neumann(const Geo &g, int kx, int ky, double2 b1, double2 b2,
+                                                 double2 &c1, double2 &c2) {
+    if (kx == 0 && ky == 0) {
+        c1 = b1;
+        c2 = make_double2(0.0, 0.0);
+        return;
+    }
+    const double kh = sqrt(g.kx[kx] * g.kx[kx] + g.ky[ky] * g.ky[ky]);
+    const double e = exp(-(kh * g.Lz));
+    const double tmp = 1.0 / (kh * (1 - exp(-(2 * kh * g.Lz))));
+    c1 = make_double2((b2.x - b1.x * e) * tmp, (b2.y - b1.y * e) * tmp);
+    c2 = make_double2((-b1.x + b2.x * e) * tmp, (-b1.y + b2.y * e) * tmp);
+}
+
+template <typename T>
+__device__ __forceinline__ double2 d2(C2<T> v) { return make_double2((double)v.x, (double)v.y); }
+
+// ----------------------------------------------------------------------------------------------
+// velocity column kernel: smem = U[3][nz][TK] + E::kBuffers * L * TK, plus small FP64 scratch
+// ----------------------------------------------------------------------------------------------
+template <typename T, class E>
+__global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename E::Desc fd, FusedArgs a, int TK) {
+    using V = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nz = g.nz, nzp = g.nzp, L = fd.L;
+    V *U = (V *)smem_raw;                       // 3 components, natural rows
+    V *X = U + (size_t)3 * nz * TK;             // FFT work
+    V *Y = X + (size_t)L * TK;
+    double2 *red = (double2 *)(X + (size_t)E::kBuffers * L * TK);  // [kThreads][2] partial wall sums
+    double2 *coef = red + 2 * kThreads;                             // [TK][2]
+    const int kx0 = blockIdx.x * TK, ky = blockIdx.y;
+    const int nv = min(TK, g.nxh - kx0);
+    auto colq = [&](int z, int c) { return fidx<T>(g, z, ky, kx0 + c); };
+    const T dt = (T)a.dt, nu = (T)a.nu, rmp = (T)a.rmp;
+
+    // ---- 1. NL forward transforms, buoyancy, filter, laplak, RK update -> U[c]
+    for (int c3 = 0; c3 < 3; c3++) {
+        const V *nl = (const V *)a.nl[c3];
+        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            X[idx] = c < nv ? nl[colq(k, c)] : mk<T>(0, 0);
+        }
+        __syncthreads();
+        fc_continuation<T>(g, X, TK);
+        __syncthreads();
+        V *R = E::run(X, Y, TK, fd, -1);
+        const V *vin = (const V *)a.vin[c3], *cold = (const V *)a.cold[c3];
+        const V *th = (const V *)a.vin[3];
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            if (c >= nv) { U[(size_t)c3 * nz * TK + idx] = mk<T>(0, 0); continue; }
+            const int kx = kx0 + c;
+            const size_t q = colq(k, c);
+            V n = R[E::pos(k, fd) * TK + c];
+            if (c3 == 2 && a.bouss) { const V t = th[q]; n = mk<T>(n.x - (T)a.xmom * t.x, n.y - (T)a.xmom * t.y); }
+            n = cscale(n, (T)g.fx[kx]);
+            n = cscale(n, (T)g.fy[ky]);
+            n = cscale(n, (T)g.fz[k]);
+            const T k2 = (T)g.kx[kx] * (T)g.kx[kx] + (T)g.ky[ky] * (T)g.ky[ky] + (T)g.kz[k] * (T)g.kz[k];
+            const V v = vin[q], cv = cold[q];
+            const V lap = cscale(v, -k2);
+            U[(size_t)c3 * nz * TK + idx] = mk<T>(cv.x + dt * (nu * lap.x - n.x) * rmp, cv.y + dt * (nu * lap.y - n.y) * rmp);
+        }
+        __syncthreads();
+    }
+    // ---- 2. goto_domain_w_boundaries, noslip_z, goto_3d_fourier for vx, vy
+    const V *pr = (const V *)a.pr;
+    for (int c3 = 0; c3 < 2; c3++) {
+        V *Uc = U + (size_t)c3 * nz * TK;
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) X[idx] = Uc[idx];
+        __syncthreads();
+        V *R = E::run(X, Y, TK, fd, +1);
+        const T inz = (T)1 / (T)nz;
+        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            V v = cscale(R[E::pos(k, fd) * TK + c], inz);
+            if ((k == 0 || k == nzp - 1) && c < nv) {
+                const int kx = kx0 + c;
+                const V p = pr[colq(k, c)];
+                v = cscale(cimk((T)(c3 == 0 ? g.kx[kx] : g.ky[ky]), p), (T)a.wall_tmp);
+                if (kx == 0 && ky == 0) v = mk<T>((T)((double)g.nx * g.ny * a.vb[(k == 0 ? 0 : 2) + c3]), (T)0);
+            }
+            Uc[idx] = v;  // physical rows, natural order (temporary)
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Uc[idx];
+        __syncthreads();
+        fc_continuation<T>(g, X, TK);
+        __syncthreads();
+        R = E::run(X, Y, TK, fd, -1);
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            Uc[idx] = R[E::pos(k, fd) * TK + c];
+        }
+        __syncthreads();
+    }
+    // ---- 3. poisson_inhomogeneous: d -> X (natural), v -= i k d, wall sums of vz/nz (FP64)
+    const double2 *wtw = (const double2 *)g.wtw;
+    {
+        const int c = threadIdx.x % TK, k0 = threadIdx.x / TK, kstep = blockDim.x / TK;
+        double2 s0 = make_double2(0, 0), s1 = make_double2(0, 0);
+        if (threadIdx.x < kstep * TK) {
+            for (int k = k0; k < nz; k += kstep) {
+                const int idx = k * TK + c;
+                const int kx = kx0 + c;
+                const T kx_ = (T)g.kx[min(kx, g.nxh - 1)], ky_ = (T)g.ky[ky], kz_ = (T)g.kz[k];
+                const T k2 = kx_ * kx_ + ky_ * ky_ + kz_ * kz_;
+                V A = U[idx], B = U[(size_t)nz * TK + idx], Cc = U[(size_t)2 * nz * TK + idx];
+                const V s = mk<T>(kx_ * A.x + ky_ * B.x + kz_ * Cc.x, kx_ * A.y + ky_ * B.y + kz_ * Cc.y);
+                V D = mk<T>(s.y / k2, -s.x / k2);
+                if (k == 0 && ky == 0 && kx == 0) D = mk<T>(0, 0);
+                A = csub(A, cimk(kx_, D));
+                B = csub(B, cimk(ky_, D));
+                Cc = csub(Cc, cimk(kz_, D));
+                U[idx] = A; U[(size_t)nz * TK + idx] = B; U[(size_t)2 * nz * TK + idx] = Cc;
+                X[idx] = D;
+                const double vr = (double)Cc.x / nz, vi = (double)Cc.y / nz;
+                const double2 w = wtw[k];
+                s0.x += vr; s0.y += vi;
+                s1.x += vr * w.x - vi * w.y;
+                s1.y += vr * w.y + vi * w.x;
+            }
+        }
+        red[2 * threadIdx.x] = s0;
+        red[2 * threadIdx.x + 1] = s1;
+    }
+    __syncthreads();
+    if (threadIdx.x < TK) {
+        const int c = threadIdx.x, kstep = blockDim.x / TK;
+        double2 b1 = make_double2(0, 0), b2 = make_double2(0, 0);
+        for (int t = 0; t < kstep; t++) {
+            const double2 p0 = red[2 * (t * TK + c)], p1 = red[2 * (t * TK + c) + 1];
+            b1.x += p0.x; b1.y += p0.y; b2.x += p1.x; b2.y += p1.y;
+        }
+        double2 c1, c2;
+        lap_coef_neumann(g, min(kx0 + c, g.nxh - 1), ky, b1, b2, c1, c2);
+        coef[2 * c] = c1;
+        coef[2 * c + 1] = c2;
+    }
+    __syncthreads();
+    // ---- 4. pressure: pr = IFFT_z(d)/nz + a(z) on the physical rows
+    {
+        V *R = E::run(X, Y, TK, fd, +1);
+        V *prw = (V *)a.pr;
+        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            if (c >= nv) continue;
+            double2 pa, pb;
+            lap_profile<T>(g, kx0 + c, ky, coef[2 * c], coef[2 * c + 1], g.z[k], pa, pb);
+            const V dv = R[E::pos(k, fd) * TK + c];
+            const T inz = (T)1 / (T)nz;
+            prw[colq(k, c)] = mk<T>((T)((double)(dv.x * inz) + pa.x), (T)((double)(dv.y * inz) + pa.y));
+        }
+        __syncthreads();
+    }
+    // ---- 5. harmonic correction: a and b profiles; the 2d rows that feed the FC-Gram
+    //         continuation are evaluated and continued in FP64, then forward transformed
+    double2 *bnd = coef + 2 * TK;  // [TK][2d]: rows 0..d-1 then nzp-d..nzp-1
+    const int d = g.oz;
+    for (int which = 0; which < 2; which++) {
+        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            double2 pa, pb;
+            lap_profile<T>(g, min(kx0 + c, g.nxh - 1), ky, coef[2 * c], coef[2 * c + 1], g.z[k], pa, pb);
+            const double2 p = which == 0 ? pa : pb;
+            X[idx] = mk<T>((T)p.x, (T)p.y);
+        }
+        for (int idx = threadIdx.x; idx < 2 * d * TK; idx += blockDim.x) {
+            const int j = idx / TK, c = idx % TK;
+            const int row = j < d ? j : nzp - 2 * d + j;
+            double2 pa, pb;
+            lap_profile<double>(g, min(kx0 + c, g.nxh - 1), ky, coef[2 * c], coef[2 * c + 1], g.z[row], pa, pb);
+            bnd[c * 2 * d + j] = which == 0 ? pa : pb;
+        }
+        __syncthreads();
+        fc_continuation_fn<T>(g, X, TK, [&](int c, int j) { return bnd[c * 2 * d + j]; },
+                              [&](int c, int j) { return bnd[c * 2 * d + d + j]; });
+        __syncthreads();
+        V *R = E::run(X, Y, TK, fd, -1);
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            const V p = R[E::pos(k, fd) * TK + c];
+            if (which == 0) {
+                const int kx = min(kx0 + c, g.nxh - 1);
+                U[idx] = csub(U[idx], cimk((T)g.kx[kx], p));
+                U[(size_t)nz * TK + idx] = csub(U[(size_t)nz * TK + idx], cimk((T)g.ky[ky], p));
+            } else {
+                U[(size_t)2 * nz * TK + idx] = csub(U[(size_t)2 * nz * TK + idx], p);
+            }
+        }
+        __syncthreads();
+    }
+    // ---- 6. store the new velocity
+    for (int c3 = 0; c3 < 3; c3++) {
+        V *vout = (V *)a.vout[c3];
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            if (c < nv) vout[colq(k, c)] = U[(size_t)c3 * nz * TK + idx];
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------------------------
+// scalar column kernel (Boussinesq): smem = Th[nz][TK] + E::kBuffers * L * TK
+// ----------------------------------------------------------------------------------------------
+template <typename T, class E>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, typename E::Desc fd, FusedArgs a, int TK) {
+    using V = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nz = g.nz, nzp = g.nzp, L = fd.L;
+    V *Th = (V *)smem_raw;
+    V *X = Th + (size_t)nz * TK;
+    V *Y = X + (size_t)L * TK;
+    const int kx0 = blockIdx.x * TK, ky = blockIdx.y;
+    const int nv = min(TK, g.nxh - kx0);
+    auto colq = [&](int z, int c) { return fidx<T>(g, z, ky, kx0 + c); };
+    const T dt = (T)a.dt, kap = (T)a.kappa, rmp = (T)a.rmp, inz = (T)1 / (T)nz;
+    // 1. NL_theta forward, heat current, filter, laplak, update
+    {
+        const V *nl = (const V *)a.nl[3];
+        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            X[idx] = c < nv ? nl[colq(k, c)] : mk<T>(0, 0);
+        }
+        __syncthreads();
+        fc_continuation<T>(g, X, TK);
+        __syncthreads();
+        V *R = E::run(X, Y, TK, fd, -1);
+        const V *vz = (const V *)a.vin[2], *th = (const V *)a.vin[3], *cold = (const V *)a.cold[3];
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            if (c >= nv) { Th[idx] = mk<T>(0, 0); continue; }
+            const int kx = kx0 + c;
+            const size_t q = colq(k, c);
+            V n = R[E::pos(k, fd) * TK + c];
+            const V w = vz[q];
+            n = mk<T>(n.x - (T)a.xtemp * w.x, n.y - (T)a.xtemp * w.y);
+            n = cscale(n, (T)g.fx[kx]);
+            n = cscale(n, (T)g.fy[ky]);
+            n = cscale(n, (T)g.fz[k]);
+            const T k2 = (T)g.kx[kx] * (T)g.kx[kx] + (T)g.ky[ky] * (T)g.ky[ky] + (T)g.kz[k] * (T)g.kz[k];
+            const V t = th[q], cv = cold[q];
+            const V lap = cscale(t, -k2);
+            Th[idx] = mk<T>(cv.x + dt * (kap * lap.x - n.x) * rmp, cv.y + dt * (kap * lap.y - n.y) * rmp);
+        }
+        __syncthreads();
+    }
+    // 2. s_imposebc (IFFT, 1/nz, walls = 0, continuation + FFT), then fc_filter
+    {
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) X[idx] = Th[idx];
+        __syncthreads();
+        V *R = E::run(X, Y, TK, fd, +1);
+        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            Th[idx] = (k == 0 || k == nzp - 1) ? mk<T>(0, 0) : cscale(R[E::pos(k, fd) * TK + c], inz);
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Th[idx];
+        __syncthreads();
+        fc_continuation<T>(g, X, TK);
+        __syncthreads();
+        R = E::run(X, Y, TK, fd, -1);
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            const int kx = min(kx0 + c, g.nxh - 1);
+            V v = R[E::pos(k, fd) * TK + c];
+            v = cscale(v, (T)g.fx[kx]);
+            v = cscale(v, (T)g.fy[ky]);
+            v = cscale(v, (T)g.fz[k]);
+            Th[idx] = v;
+        }
+        __syncthreads();
+    }
+    // 3. c2r -> /(nx ny nz) -> r2c: z-inverse and 1/nz here; kx = 0 and nx/2 go to the side buffer
+    {
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) X[idx] = Th[idx];
+        __syncthreads();
+        V *R = E::run(X, Y, TK, fd, +1);
+        V *side = (V *)a.side;
+        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            const V v = cscale(R[E::pos(k, fd) * TK + c], inz);
+            Th[idx] = v;
+            const int kx = kx0 + c;
+            if (c < nv && (kx == 0 || kx == g.nxh - 1))
+                side[((size_t)(kx == 0 ? 0 : 1) * g.ny + ky) * nzp + k] = v;
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Th[idx];
+        __syncthreads();
+        fc_continuation<T>(g, X, TK);
+        __syncthreads();
+        R = E::run(X, Y, TK, fd, -1);
+        V *out = (V *)a.vout[3];
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            const int kx = kx0 + c;
+            if (c < nv && kx != 0 && kx != g.nxh - 1) out[colq(k, c)] = R[E::pos(k, fd) * TK + c];
+        }
+    }
+}
+
+// kx = 0 and kx = nx/2 columns of the theta round trip: (X(ky) + conj X(-ky))/2, then continuation
+// and forward z transform.  One block per (kx column, ky pair); two columns per block.
+template <typename T, class E>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_theta_herm(Geo g, typename E::Desc fd, FusedArgs a) {
+    using V = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nzp = g.nzp, nz = g.nz, L = fd.L;
+    const int TK = 2;
+    V *X = (V *)smem_raw, *Y = X + (size_t)L * TK;
+    const int sel = blockIdx.y;                 // 0: kx = 0, 1: kx = nx/2
+    const int kx = sel == 0 ? 0 : g.nxh - 1;
+    const int ky = blockIdx.x, kym = (g.ny - ky) % g.ny;
+    if (ky > kym) return;                       // each pair once (ky <= -ky mod ny)
+    const V *side = (const V *)a.side;
+    const V *s1 = side + ((size_t)sel * g.ny + ky) * nzp, *s2 = side + ((size_t)sel * g.ny + kym) * nzp;
+    for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
+        const int k = idx / TK, c = idx % TK;
+        const V p = s1[k], m = s2[k];
+        // column c = 0 holds ky, c = 1 holds -ky
+        const V h = c == 0 ? mk<T>((T)0.5 * (p.x + m.x), (T)0.5 * (p.y - m.y)) : mk<T>((T)0.5 * (m.x + p.x), (T)0.5 * (m.y - p.y));
+        X[idx] = h;
+    }
+    __syncthreads();
+    fc_continuation<T>(g, X, TK);
+    __syncthreads();
+    V *R = E::run(X, Y, TK, fd, -1);
+    V *out = (V *)a.vout[3];
+    for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+        const int k = idx / TK, c = idx % TK;
+        if (c == 1 && kym == ky) continue;
+        out[fidx<T>(g, k, c == 0 ? ky : kym, kx)] = R[E::pos(k, fd) * TK + c];
+    }
+}
+
+}  // namespace sg

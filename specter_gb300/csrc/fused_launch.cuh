@@ -1,0 +1,56 @@
+// Launch helpers of the fused column kernels, shared by the generic and the four-step TUs.
+#pragma once
+
+#include <string>
+
+#include "fused_kernels.cuh"
+
+namespace sg {
+
+enum FusedKernel { kFusedVelocity = 0, kFusedTheta = 1, kFusedHerm = 2 };
+
+template <typename T, class E>
+int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int which, double bytes) {
+    const size_t es = sizeof(C2<T>);
+    const size_t L = (size_t)fd.L;
+    const int d = P.oz;
+    auto smem = [&](int tk) -> size_t {
+        if (which == kFusedVelocity)
+            return (3 * (size_t)P.nz + E::kBuffers * L) * tk * es + (2 * (size_t)kThreads + (size_t)tk * (2 + 2 * d)) * 16;
+        if (which == kFusedTheta) return ((size_t)P.nz + E::kBuffers * L) * tk * es;
+        return E::kBuffers * L * 2 * es;
+    };
+    int tk = 2;
+    if (which != kFusedHerm) {
+        tk = 0;
+        const size_t budget = which == kFusedVelocity ? 200 * 1024 : 110 * 1024;
+        for (int t : {16, 8, 4, 2, 1})
+            if (smem(t) <= budget) { tk = t; break; }
+        if (!tk) { set_error("z length too large for the fused column kernels"); return ERR_SHAPE; }
+    }
+    const size_t sm = smem(tk);
+    const char *name = which == kFusedVelocity ? "fused_velocity" : which == kFusedTheta ? "fused_theta" : "theta_herm";
+    P.prof_begin(name, bytes);
+    if (which == kFusedVelocity) {
+        auto k = k_fused_velocity<T, E>;
+        if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k<<<dim3(cdiv(P.nxh, tk), P.ny), kThreads, sm, P.stream>>>(P.geo, fd, a, tk);
+    } else if (which == kFusedTheta) {
+        auto k = k_fused_theta<T, E>;
+        if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k<<<dim3(cdiv(P.nxh, tk), P.ny), kThreads, sm, P.stream>>>(P.geo, fd, a, tk);
+    } else {
+        auto k = k_theta_herm<T, E>;
+        if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k<<<dim3(P.ny, 2), kThreads, sm, P.stream>>>(P.geo, fd, a);
+    }
+    P.prof_end();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { set_error(std::string(name) + ": " + cudaGetErrorString(e)); return ERR_CUDA; }
+    return OK;
+}
+
+// four-step variant (fused_fast_f32.cu); kNoFast (-1) when the plan has no four-step z table
+int fast_fused(Plan &P, const FusedArgs &a, int which, double bytes);
+
+}  // namespace sg

@@ -6,9 +6,16 @@
 // every pass is a batched strided FFT whose loads and stores are coalesced along kx,
 // so no global transpose is needed: the x/y/z passes read (TK kx) x (length) tiles.
 // Physical (real) fields use the reference layout r[(z*ny + y)*nx + x].
+//
+// Every pass kernel is templated on an FFT policy E:
+//   GenericFFT<T>          Stockham / Bluestein over two smem buffers, any length (fft.cuh)
+//   FourStep<T, L1, L2>    register four-step over one smem buffer, L = L1*L2 (fft4.cuh)
+// E::run transforms rows [0, n) held in X and returns the buffer with the result;
+// E::pos(k) is the smem row that holds output k.
 #pragma once
 
 #include "fft.cuh"
+#include "fft4.cuh"
 #include "plan.h"
 
 namespace sg {
@@ -20,6 +27,35 @@ template <typename T>
 __device__ __forceinline__ size_t fidx(const Geo &g, int z, int ky, int kx) {
     return ((size_t)z * g.ny + ky) * g.ldx + kx;
 }
+
+template <typename T>
+struct GenericFFT {
+    using Desc = FFTDesc;
+    static constexpr int kBuffers = 2;
+    static constexpr int kMinBlocks = 1;
+    static __device__ __forceinline__ C2<T> *run(C2<T> *X, C2<T> *Y, int B, const Desc &d, int sign) {
+        return fft_exec<T>(X, Y, B, d, sign);
+    }
+    static __device__ __forceinline__ int pos(int k, const Desc &) { return k; }
+};
+
+template <typename T, int L1, int L2>
+struct FourStep {
+    using Desc = FFT4Desc;
+    static constexpr int kBuffers = 1;
+    static constexpr int kMinBlocks = 2;  // cap registers at 128 so two blocks share an SM
+    static __device__ __forceinline__ C2<T> *run(C2<T> *X, C2<T> *, int B, const Desc &d, int sign) {
+        if (d.blue) {
+            if (sign < 0) fft4_bluestein<T, L1, L2, -1>(X, B, d);
+            else fft4_bluestein<T, L1, L2, +1>(X, B, d);
+        } else {
+            if (sign < 0) fft4_np<T, L1, L2, -1>(X, B, d);
+            else fft4_np<T, L1, L2, +1>(X, B, d);
+        }
+        return X;
+    }
+    static __device__ __forceinline__ int pos(int k, const Desc &d) { return d.blue ? k : perm_pos<L1, L2>(k); }
+};
 
 // ---------------------------------------------------------------------------------
 // z pass, inverse: out0 = scale * IFFT_z(in) (+ add), out1 = scale * IFFT_z(i kz in).
@@ -35,8 +71,8 @@ struct ZInvArgs {
     double scale;
 };
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_z_inverse(Geo g, FFTDesc fd, ZInvArgs a, int TK) {
+template <typename T, class E>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_inverse(Geo g, typename E::Desc fd, ZInvArgs a, int TK) {
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * TK;
@@ -54,12 +90,12 @@ __global__ void __launch_bounds__(kThreads) k_z_inverse(Geo g, FFTDesc fd, ZInvA
             X[idx] = v;
         }
         __syncthreads();
-        V *R = fft_exec<T>(X, Y, TK, fd, +1);
+        V *R = E::run(X, Y, TK, fd, +1);
         const V *add = (const V *)a.add[f];
         for (int idx = threadIdx.x; idx < a.nrows * TK; idx += blockDim.x) {
             const int k = idx / TK, c = idx % TK;
             if (c >= nv) continue;
-            V v = R[idx];
+            V v = R[E::pos(k, fd) * TK + c];
             if (k < a.scale_rows) v = cscale(v, (T)a.scale);
             const size_t q = fidx<T>(g, k, ky, kx0 + c);
             if (pass == 0 && add) v = cadd(v, add[q]);
@@ -100,8 +136,8 @@ __device__ __forceinline__ void fc_continuation(const Geo &g, C2<T> *X, int TK) 
     }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_z_forward(Geo g, FFTDesc fd, ZFwdArgs a, int TK) {
+template <typename T, class E>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_forward(Geo g, typename E::Desc fd, ZFwdArgs a, int TK) {
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * TK;
@@ -119,10 +155,10 @@ __global__ void __launch_bounds__(kThreads) k_z_forward(Geo g, FFTDesc fd, ZFwdA
     __syncthreads();
     fc_continuation<T>(g, X, TK);
     __syncthreads();
-    V *R = fft_exec<T>(X, Y, TK, fd, -1);
+    V *R = E::run(X, Y, TK, fd, -1);
     for (int idx = threadIdx.x; idx < g.nz * TK; idx += blockDim.x) {
         const int k = idx / TK, c = idx % TK;
-        if (c < nv) out[fidx<T>(g, k, ky, kx0 + c)] = R[idx];
+        if (c < nv) out[fidx<T>(g, k, ky, kx0 + c)] = R[E::pos(k, fd) * TK + c];
     }
 }
 
@@ -137,8 +173,8 @@ struct YArgs {
     double scale;
 };
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_y_pass(Geo g, FFTDesc fd, YArgs a, int TK) {
+template <typename T, class E>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass(Geo g, typename E::Desc fd, YArgs a, int TK) {
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * TK;
@@ -156,11 +192,11 @@ __global__ void __launch_bounds__(kThreads) k_y_pass(Geo g, FFTDesc fd, YArgs a,
             X[idx] = v;
         }
         __syncthreads();
-        V *R = fft_exec<T>(X, Y, TK, fd, a.sign);
+        V *R = E::run(X, Y, TK, fd, a.sign);
         for (int idx = threadIdx.x; idx < g.ny * TK; idx += blockDim.x) {
             const int k = idx / TK, c = idx % TK;
             if (c < nv) {
-                V v = R[idx];
+                V v = R[E::pos(k, fd) * TK + c];
                 if (a.scale != 1.0) v = cscale(v, (T)a.scale);
                 out[fidx<T>(g, z, k, kx0 + c)] = v;
             }
@@ -173,7 +209,7 @@ __global__ void __launch_bounds__(kThreads) k_y_pass(Geo g, FFTDesc fd, YArgs a,
 // x pass helpers: real rows of length nx = 2H through a complex FFT of length H.
 // ---------------------------------------------------------------------------------
 
-// Build Z (H rows) for a C2R from the half spectrum S (nxh rows, RB columns):
+// Build Z (H rows, natural order) for a C2R from the half spectrum S (nxh rows, RB columns):
 // Z_k = (X_k + conj X_{H-k}) + i e^{+2 pi i k/nx} (X_k - conj X_{H-k}); Im X_0 = Im X_H = 0.
 template <typename T>
 __device__ __forceinline__ void c2r_pre(const Geo &g, const C2<T> *S, C2<T> *Z, int RB) {
@@ -193,16 +229,16 @@ __device__ __forceinline__ void c2r_pre(const Geo &g, const C2<T> *S, C2<T> *Z, 
     }
 }
 
-// From Z = FFT_H(packed real row), write the half spectrum X_0..X_H (scaled) into S:
-// X_k = (Z_k + conj Z_{H-k})/2 - (i/2) e^{-2 pi i k/nx} (Z_k - conj Z_{H-k}).
-template <typename T>
-__device__ __forceinline__ void r2c_post(const Geo &g, const C2<T> *Z, C2<T> *S, int RB) {
+// From Z = FFT_H(packed real row) (output k at smem row E::pos(k)), write the half spectrum
+// X_0..X_H into S:  X_k = (Z_k + conj Z_{H-k})/2 - (i/2) e^{-2 pi i k/nx} (Z_k - conj Z_{H-k}).
+template <typename T, class E>
+__device__ __forceinline__ void r2c_post(const Geo &g, const typename E::Desc &fd, const C2<T> *Z, C2<T> *S, int RB) {
     using V = C2<T>;
     const V *xtw = (const V *)g.xtw;
     const int H = g.H;
     for (int idx = threadIdx.x; idx < (H + 1) * RB; idx += blockDim.x) {
         const int k = idx / RB, r = idx % RB;
-        const V zk = Z[(k % H) * RB + r], zm = cconj(Z[((H - k) % H) * RB + r]);
+        const V zk = Z[E::pos(k % H, fd) * RB + r], zm = cconj(Z[E::pos((H - k) % H, fd) * RB + r]);
         const V e = cadd(zk, zm), d = csub(zk, zm);
         const V t = cmul(d, __ldg(xtw + k));
         S[idx] = mk<T>((T)0.5 * (e.x + t.y), (T)0.5 * (e.y - t.x));
@@ -217,11 +253,11 @@ struct XArgs {
     double scale;
 };
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_x_r2c(Geo g, FFTDesc fd, XArgs a, int RB) {
+template <typename T, class E>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_r2c(Geo g, typename E::Desc fd, XArgs a, int RB) {
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * RB, *S = Y + (size_t)fd.L * RB;
+    V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * RB, *S = X + (size_t)E::kBuffers * fd.L * RB;
     const int f = blockIdx.z;
     const int row0 = blockIdx.x * RB, nrows = a.nrows * g.ny;
     const T *in = (const T *)a.in[f];
@@ -237,8 +273,8 @@ __global__ void __launch_bounds__(kThreads) k_x_r2c(Geo g, FFTDesc fd, XArgs a, 
         X[idx] = v;
     }
     __syncthreads();
-    V *R = fft_exec<T>(X, Y, RB, fd, -1);
-    r2c_post<T>(g, R, S, RB);
+    V *R = E::run(X, Y, RB, fd, -1);
+    r2c_post<T, E>(g, fd, R, S, RB);
     __syncthreads();
     for (int idx = threadIdx.x; idx < g.nxh * RB; idx += blockDim.x) {
         const int r = idx / g.nxh, k = idx % g.nxh;
@@ -251,11 +287,11 @@ __global__ void __launch_bounds__(kThreads) k_x_r2c(Geo g, FFTDesc fd, XArgs a, 
 }
 
 // x pass C2R: r[row] = IFFT_x(in[row]) (Hermitian half spectrum; Im of kx=0, nx/2 ignored)
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_x_c2r(Geo g, FFTDesc fd, XArgs a, int RB) {
+template <typename T, class E>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_c2r(Geo g, typename E::Desc fd, XArgs a, int RB) {
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * RB, *S = Y + (size_t)fd.L * RB;
+    V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * RB, *S = X + (size_t)E::kBuffers * fd.L * RB;
     const int f = blockIdx.z;
     const int row0 = blockIdx.x * RB, nrows = a.nrows * g.ny;
     const V *in = (const V *)a.in[f];
@@ -269,12 +305,12 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Geo g, FFTDesc fd, XArgs a, 
     __syncthreads();
     c2r_pre<T>(g, S, X, RB);
     __syncthreads();
-    V *R = fft_exec<T>(X, Y, RB, fd, +1);
+    V *R = E::run(X, Y, RB, fd, +1);
     const int H = g.H;
     for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
         const int r = idx / H, m = idx % H;
         if (row0 + r < nrows) {
-            V v = R[m * RB + r];
+            V v = R[E::pos(m, fd) * RB + r];
             if (a.scale != 1.0) v = cscale(v, (T)a.scale);
             T *p = out + (size_t)(row0 + r) * g.nx + 2 * m;
             p[0] = v.x;
@@ -286,9 +322,9 @@ __global__ void __launch_bounds__(kThreads) k_x_c2r(Geo g, FFTDesc fd, XArgs a, 
 // ---------------------------------------------------------------------------------
 // Fused x pass for the nonlinear terms (gradre, pseudospec_hd.f90:209-319, and advect,
 // pseudospec_phd.f90:23-113).  Per (y,z) row, inputs are the y-inverse-transformed rows
-// U_j (velocity), DY_i = d/dy v_i, DZ_i = d/dz v_i (and TH, DYT, DZT for the scalar).
-// d/dx is i*kx applied to the spectral row.  Physical rows stay packed as H complex
-// numbers (x_{2m} + i x_{2m+1}); products act on real and imaginary parts separately.
+// U_j (velocity), DY_i = d/dy v_i, DZ_i = d/dz v_i (and theta's).  d/dx is i*kx applied
+// to the spectral row.  Physical rows stay packed as H complex numbers
+// (x_{2m} + i x_{2m+1}); products act on real and imaginary parts separately.
 //   NL_i = ((u_x d_x v_i + u_y d_y v_i) + u_z d_z v_i) * 1/(nx ny nz)^2
 // then a forward R2C of each NL_i.
 // ---------------------------------------------------------------------------------
@@ -314,39 +350,42 @@ __device__ __forceinline__ void load_row_spec(const Geo &g, const C2<T> *in, C2<
     }
 }
 
-// C2R of a spectral row set held in S into P (H x RB packed physical)
-template <typename T>
-__device__ __forceinline__ void c2r_rows(const Geo &g, const FFTDesc &fd, C2<T> *S, C2<T> *X, C2<T> *Y, C2<T> *P, int RB) {
+// C2R of a spectral row set held in S into P (H x RB packed physical, natural order)
+template <typename T, class E>
+__device__ __forceinline__ void c2r_rows(const Geo &g, const typename E::Desc &fd, C2<T> *S, C2<T> *X, C2<T> *Y,
+                                         C2<T> *P, int RB) {
     __syncthreads();
     c2r_pre<T>(g, S, X, RB);
     __syncthreads();
-    C2<T> *R = fft_exec<T>(X, Y, RB, fd, +1);
-    for (int idx = threadIdx.x; idx < g.H * RB; idx += blockDim.x) P[idx] = R[idx];
+    C2<T> *R = E::run(X, Y, RB, fd, +1);
+    for (int idx = threadIdx.x; idx < g.H * RB; idx += blockDim.x) {
+        const int m = idx / RB, r = idx % RB;
+        P[idx] = R[E::pos(m, fd) * RB + r];
+    }
     __syncthreads();
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_x_nonlinear(Geo g, FFTDesc fd, XNLArgs a, int RB) {
+template <typename T, class E>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, typename E::Desc fd, XNLArgs a, int RB) {
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int H = g.H, L = fd.L;
     V *X = (V *)smem_raw;
     V *Y = X + (size_t)L * RB;
-    V *S = Y + (size_t)L * RB;                 // nxh * RB spectral row staging
+    V *S = X + (size_t)E::kBuffers * L * RB;   // nxh * RB spectral row staging
     V *U = S + (size_t)g.nxh * RB;              // 3 * H * RB physical velocity rows
     V *P = U + (size_t)3 * H * RB;              // H * RB product operand
     V *A = P + (size_t)H * RB;                  // (c1-c0) * H * RB accumulators
     const int c0 = a.c0, c1 = a.c1;
     const int row0 = blockIdx.x * RB, nrows = a.nrows * g.ny;
-    // velocity rows; after each, the x-derivative term of the same component
     for (int j = 0; j < 3; j++) {
         load_row_spec<T>(g, (const V *)a.u[j], S, row0, nrows, RB, 0);
-        c2r_rows<T>(g, fd, S, X, Y, U + (size_t)j * H * RB, RB);
+        c2r_rows<T, E>(g, fd, S, X, Y, U + (size_t)j * H * RB, RB);
     }
     // term 1: u_x * d/dx v_i (and theta)
     for (int i = c0; i < c1; i++) {
         load_row_spec<T>(g, (const V *)a.u[i], S, row0, nrows, RB, 1);
-        c2r_rows<T>(g, fd, S, X, Y, P, RB);
+        c2r_rows<T, E>(g, fd, S, X, Y, P, RB);
         for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
             const V u = U[idx], p = P[idx];
             A[(size_t)(i - c0) * H * RB + idx] = mk<T>(u.x * p.x, u.y * p.y);
@@ -355,7 +394,7 @@ __global__ void __launch_bounds__(kThreads) k_x_nonlinear(Geo g, FFTDesc fd, XNL
     // term 2: + u_y * d/dy v_i
     for (int i = c0; i < c1; i++) {
         load_row_spec<T>(g, (const V *)a.dy[i], S, row0, nrows, RB, 0);
-        c2r_rows<T>(g, fd, S, X, Y, P, RB);
+        c2r_rows<T, E>(g, fd, S, X, Y, P, RB);
         for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
             const V u = U[(size_t)H * RB + idx], p = P[idx];
             V &acc = A[(size_t)(i - c0) * H * RB + idx];
@@ -366,15 +405,15 @@ __global__ void __launch_bounds__(kThreads) k_x_nonlinear(Geo g, FFTDesc fd, XNL
     const T tmp = (T)a.tmp;
     for (int i = c0; i < c1; i++) {
         load_row_spec<T>(g, (const V *)a.dz[i], S, row0, nrows, RB, 0);
-        c2r_rows<T>(g, fd, S, X, Y, P, RB);
+        c2r_rows<T, E>(g, fd, S, X, Y, P, RB);
         for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
             const V u = U[(size_t)2 * H * RB + idx], p = P[idx];
             const V acc = A[(size_t)(i - c0) * H * RB + idx];
             X[idx] = mk<T>((acc.x + u.x * p.x) * tmp, (acc.y + u.y * p.y) * tmp);
         }
         __syncthreads();
-        V *R = fft_exec<T>(X, Y, RB, fd, -1);
-        r2c_post<T>(g, R, S, RB);
+        V *R = E::run(X, Y, RB, fd, -1);
+        r2c_post<T, E>(g, fd, R, S, RB);
         __syncthreads();
         V *out = (V *)a.out[i];
         for (int idx = threadIdx.x; idx < g.nxh * RB; idx += blockDim.x) {

@@ -26,7 +26,10 @@ template <typename T> struct Ops {
     static int laplak(Plan &P, const void *a, void *b);
     static int curlk(Plan &P, const void *a, const void *b, void *c, int dir);
     static int fc_filter(Plan &P, void *a);
-    static int nonlinear(Plan &P, const void *const v[3], const void *th, void *const out[4], int c0, int c1);
+    // NL terms of components [c0, c1) (0..2 velocity, 3 scalar) into out[] (spectral); with
+    // `mixed` given, stops before the z transform and returns the mixed-domain NL (scratch)
+    static int nonlinear(Plan &P, const void *const v[3], const void *th, void *const out[4], int c0, int c1,
+                         const void **mixed = nullptr);
     static int energy(Plan &P, const void *a, const void *b, const void *c, int kin, double *out);
     static int helicity(Plan &P, const void *a, const void *b, const void *c, double *out);
     static int cross(Plan &P, const void *const A[3], const void *const B[3], int kin, double *out);

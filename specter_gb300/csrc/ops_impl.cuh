@@ -3,6 +3,7 @@
 #include <string>
 #include <vector>
 
+#include "fast.h"
 #include "kernels.cuh"
 #include "kernels_elem.cuh"
 #include "ops.h"
@@ -49,6 +50,17 @@ static int elem_blocks(const Plan &P, int rows) {
     return (int)(b < 1 ? 1 : b);
 }
 
+// Brackets one kernel launch for the plan's launch counter and (when enabled) its event
+// profiler.  `bytes` is the launch's algorithmic traffic: each input element read once and
+// each output element written once.
+struct Launch {
+    Plan &P;
+    Launch(Plan &p, const char *name, double bytes) : P(p) { P.prof_begin(name, bytes); }
+    ~Launch() { P.prof_end(); }
+};
+
+static double cplx_rows(const Plan &P, double rows) { return rows * P.ny * P.nxh * (double)P.elt(); }
+
 // ------------------------------------------------------------------------- launchers
 // Tile widths (kx columns per block for the y/z passes, rows per block for the x pass) are
 // runtime values: the largest power of two whose ping-pong buffers fit the smem budget.
@@ -59,8 +71,14 @@ static int launch_z_inverse(Plan &P, const ZInvArgs &a, int nf) {
     const int tk = pick_tile(2 * (size_t)P.tz.d.L * es);
     if (!tk) { set_error("z length too large for shared memory"); return ERR_SHAPE; }
     const size_t sm = 2 * (size_t)P.tz.d.L * tk * es;
-    set_smem(k_z_inverse<T>, sm);
-    k_z_inverse<T><<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz.d, a, tk);
+    double bytes = 0;
+    for (int f = 0; f < nf; f++)
+        bytes += cplx_rows(P, P.nz) + cplx_rows(P, a.nrows) * ((a.out0[f] ? 1 : 0) + (a.out1[f] ? 1 : 0) + (a.add[f] ? 1 : 0));
+    const int fst = fast_z_inverse(P, a, nf, bytes);
+    if (fst != kNoFast) return fst;
+    set_smem(k_z_inverse<T, GenericFFT<T>>, sm);
+    Launch L(P, "z_inverse", bytes);
+    k_z_inverse<T, GenericFFT<T>><<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz.d, a, tk);
     return check_launch("z_inverse");
 }
 
@@ -70,8 +88,12 @@ static int launch_z_forward(Plan &P, const ZFwdArgs &a, int nf) {
     const int tk = pick_tile(2 * (size_t)P.tz.d.L * es);
     if (!tk) { set_error("z length too large for shared memory"); return ERR_SHAPE; }
     const size_t sm = 2 * (size_t)P.tz.d.L * tk * es;
-    set_smem(k_z_forward<T>, sm);
-    k_z_forward<T><<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz.d, a, tk);
+    const double bytes = nf * (cplx_rows(P, P.nzp) + cplx_rows(P, P.nz));
+    const int fst = fast_z_forward(P, a, nf, bytes);
+    if (fst != kNoFast) return fst;
+    set_smem(k_z_forward<T, GenericFFT<T>>, sm);
+    Launch L(P, "z_forward", bytes);
+    k_z_forward<T, GenericFFT<T>><<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz.d, a, tk);
     return check_launch("z_forward");
 }
 
@@ -81,8 +103,13 @@ static int launch_y(Plan &P, const YArgs &a, int nf, int nplanes) {
     const int tk = pick_tile(2 * (size_t)P.ty.d.L * es);
     if (!tk) { set_error("y length too large for shared memory"); return ERR_SHAPE; }
     const size_t sm = 2 * (size_t)P.ty.d.L * tk * es;
-    set_smem(k_y_pass<T>, sm);
-    k_y_pass<T><<<dim3(cdiv(P.nxh, tk), nplanes, nf), kThreads, sm, P.stream>>>(P.geo, P.ty.d, a, tk);
+    double bytes = 0;
+    for (int f = 0; f < nf; f++) bytes += cplx_rows(P, nplanes) * (1 + (a.out0[f] ? 1 : 0) + (a.out1[f] ? 1 : 0));
+    const int fst = fast_y(P, a, nf, nplanes, bytes);
+    if (fst != kNoFast) return fst;
+    set_smem(k_y_pass<T, GenericFFT<T>>, sm);
+    Launch L(P, a.sign < 0 ? "y_forward" : "y_inverse", bytes);
+    k_y_pass<T, GenericFFT<T>><<<dim3(cdiv(P.nxh, tk), nplanes, nf), kThreads, sm, P.stream>>>(P.geo, P.ty.d, a, tk);
     return check_launch("y_pass");
 }
 
@@ -94,12 +121,18 @@ static int launch_x(Plan &P, const XArgs &a, int nf, bool r2c) {
     if (!rb) { set_error("x length too large for shared memory"); return ERR_SHAPE; }
     const size_t sm = per * rb;
     const dim3 grid(cdiv(a.nrows * P.ny, rb), 1, nf);
+    const double rows = (double)a.nrows * P.ny;
+    const double bytes = nf * rows * ((double)P.nxh * P.elt() + (double)P.nx * P.rel());
+    const int fst = fast_x(P, a, nf, r2c, bytes);
+    if (fst != kNoFast) return fst;
     if (r2c) {
-        set_smem(k_x_r2c<T>, sm);
-        k_x_r2c<T><<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx.d, a, rb);
+        set_smem(k_x_r2c<T, GenericFFT<T>>, sm);
+        Launch L(P, "x_r2c", bytes);
+        k_x_r2c<T, GenericFFT<T>><<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx.d, a, rb);
     } else {
-        set_smem(k_x_c2r<T>, sm);
-        k_x_c2r<T><<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx.d, a, rb);
+        set_smem(k_x_c2r<T, GenericFFT<T>>, sm);
+        Launch L(P, "x_c2r", bytes);
+        k_x_c2r<T, GenericFFT<T>><<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx.d, a, rb);
     }
     return check_launch(r2c ? "x_r2c" : "x_c2r");
 }
@@ -111,8 +144,15 @@ static int launch_x_nl(Plan &P, const XNLArgs &a) {
     const int rb = pick_tile(per);
     if (!rb) { set_error("x length too large for shared memory"); return ERR_SHAPE; }
     const size_t sm = per * rb;
-    set_smem(k_x_nonlinear<T>, sm);
-    k_x_nonlinear<T><<<dim3(cdiv(a.nrows * P.ny, rb)), kThreads, sm, P.stream>>>(P.geo, P.tx.d, a, rb);
+    const int nc = a.c1 - a.c0;
+    // rows read: 3 velocity rows (+ theta), d/dy and d/dz rows of each component; written: NL rows
+    const double nin = 3 + (a.c1 == 4 ? 1 : 0) + 2 * nc;
+    const double bytes = cplx_rows(P, a.nrows) * (nin + nc);
+    const int fst = fast_x_nl(P, a, bytes);
+    if (fst != kNoFast) return fst;
+    set_smem(k_x_nonlinear<T, GenericFFT<T>>, sm);
+    Launch L(P, "x_nonlinear", bytes);
+    k_x_nonlinear<T, GenericFFT<T>><<<dim3(cdiv(a.nrows * P.ny, rb)), kThreads, sm, P.stream>>>(P.geo, P.tx.d, a, rb);
     return check_launch("x_nonlinear");
 }
 
@@ -144,7 +184,7 @@ static int finish_reduce(Plan &P, int nblocks, int per, double *out) {
 template <typename T>
 static int reduce(Plan &P, const RedArgs &a, double *out) {
     const int nb = 304;
-    k_reduce<T><<<nb, kThreads, 0, P.stream>>>(P.geo, a, P.dred);
+    { Launch L_(P, "reduce", a.nf * cplx_rows(P, a.z1)); k_reduce<T><<<nb, kThreads, 0, P.stream>>>(P.geo, a, P.dred); }
     SG_TRY(check_launch("reduce"));
     return finish_reduce(P, nb, 1, out);
 }
@@ -210,23 +250,23 @@ template <typename T> int Ops<T>::fftp3d_c2r(Plan &P, void *cin, void *rout) {
 
 template <typename T> int Ops<T>::derivk(Plan &P, const void *a, void *b, int dir) {
     if (dir < 1 || dir > 3) { set_error("derivk: dir must be 1, 2 or 3"); return ERR_ARG; }
-    k_derivk<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a), F<T>(b), dir);
+    { Launch L_(P, "derivk", 2.0 * cplx_rows(P, P.nz)); k_derivk<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a), F<T>(b), dir); }
     return check_launch("derivk");
 }
 
 template <typename T> int Ops<T>::laplak(Plan &P, const void *a, void *b) {
-    k_laplak<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a), F<T>(b));
+    { Launch L_(P, "laplak", 2.0 * cplx_rows(P, P.nz)); k_laplak<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a), F<T>(b)); }
     return check_launch("laplak");
 }
 
 template <typename T> int Ops<T>::curlk(Plan &P, const void *a, const void *b, void *c, int dir) {
     if (dir < 1 || dir > 3) { set_error("curlk: dir must be 1, 2 or 3"); return ERR_ARG; }
-    k_curlk<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a), F<T>(b), F<T>(c), dir);
+    { Launch L_(P, "curlk", 3.0 * cplx_rows(P, P.nz)); k_curlk<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a), F<T>(b), F<T>(c), dir); }
     return check_launch("curlk");
 }
 
 template <typename T> int Ops<T>::fc_filter(Plan &P, void *a) {
-    k_filter<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a));
+    { Launch L_(P, "filter", 2.0 * cplx_rows(P, P.nz)); k_filter<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a)); }
     return check_launch("fc_filter");
 }
 
@@ -237,7 +277,8 @@ template <typename T> int Ops<T>::fc_filter(Plan &P, void *a) {
 // Products are formed on the physical rows z < nz - Cz only; rows above are rebuilt
 // by the continuation, exactly as in the reference.
 template <typename T>
-int Ops<T>::nonlinear(Plan &P, const void *const v[3], const void *th, void *const out[4], int c0, int c1) {
+int Ops<T>::nonlinear(Plan &P, const void *const v[3], const void *th, void *const out[4], int c0, int c1,
+                      const void **mixed) {
     void *S[16];
     SG_TRY(scratch(P, 16, S));
     const int nzp = P.nzp;
@@ -287,11 +328,15 @@ int Ops<T>::nonlinear(Plan &P, const void *const v[3], const void *th, void *con
     nf = 0;
     for (int c = c0; c < c1; c++) {
         y3.in[nf] = S[c]; y3.out0[nf] = S[c]; y3.out1[nf] = nullptr;
-        zf.in[nf] = S[c]; zf.out[nf] = out[c];
+        zf.in[nf] = S[c]; zf.out[nf] = out ? out[c] : nullptr;
         nf++;
     }
     y3.sign = -1; y3.scale = 1.0;
     SG_TRY(launch_y<T>(P, y3, nf, nzp));
+    if (mixed) {  // the caller finishes the z direction itself (fused stage kernels)
+        for (int c = 0; c < 4; c++) mixed[c] = S[c];
+        return OK;
+    }
     zf.in_scale = 1.0;
     return launch_z_forward<T>(P, zf, nf);
 }
@@ -390,7 +435,7 @@ template <typename T> int Ops<T>::cross(Plan &P, const void *const A[3], const v
 template <typename T> int Ops<T>::divergence(Plan &P, const void *a, const void *b, const void *c, double *out) {
     void *S[2];
     SG_TRY(scratch(P, 2, S));
-    k_div<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a), F<T>(b), F<T>(c), F<T>(S[1]));
+    { Launch L_(P, "div", 4.0 * cplx_rows(P, P.nz)); k_div<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a), F<T>(b), F<T>(c), F<T>(S[1])); }
     SG_TRY(check_launch("divergence"));
     const void *in[1] = {S[1]};
     SG_TRY(zinv_scratch<T>(P, in, 1, S));
@@ -408,7 +453,7 @@ template <typename T> int Ops<T>::variance(Plan &P, const void *a, int kin, doub
     SG_TRY(scratch(P, 2, S));
     const void *src = a;
     if (kin == 0) {
-        k_kk2_mul<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a), F<T>(S[1]));
+        { Launch L_(P, "kk2_mul", 2.0 * cplx_rows(P, P.nz)); k_kk2_mul<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a), F<T>(S[1])); }
         SG_TRY(check_launch("variance"));
         src = S[1];
     }
@@ -444,7 +489,7 @@ static double2 *plan_bc(Plan &P, int i) { return (double2 *)P.scratch_field(kScr
 
 template <typename T>
 static int wall_eval(Plan &P, const void *in, double scale, double2 *bc, int neg) {
-    k_wall_eval<T><<<dim3(cdiv(P.nxh, 64), P.ny), 64, 0, P.stream>>>(P.geo, F<T>(in), scale, plan_wtw(P), bc, neg);
+    { Launch L_(P, "wall_eval", cplx_rows(P, P.nz)); k_wall_eval<T><<<dim3(cdiv(P.nxh, 64), P.ny), 64, 0, P.stream>>>(P.geo, F<T>(in), scale, plan_wtw(P), bc, neg); }
     return check_launch("wall_eval");
 }
 
@@ -455,7 +500,7 @@ template <typename T> int Ops<T>::bouncheck_z(Plan &P, const void *a, const void
     SG_TRY(wall_eval<T>(P, a, 1.0, bcA, 0));
     if (b) SG_TRY(wall_eval<T>(P, b, 1.0, bcB, 0));
     const int nb = 152;
-    k_reduce_walls<<<nb, kThreads, 0, P.stream>>>(P.geo, bcA, b ? bcB : nullptr, P.dred);
+    { Launch L_(P, "reduce_walls", 64.0 * P.nxh * P.ny); k_reduce_walls<<<nb, kThreads, 0, P.stream>>>(P.geo, bcA, b ? bcB : nullptr, P.dred); }
     SG_TRY(check_launch("bouncheck_z"));
     double r[2];
     SG_TRY(finish_reduce(P, nb, 2, r));
@@ -473,12 +518,12 @@ template <typename T> int Ops<T>::sol_project(Plan &P, void *a, void *b, void *c
     SG_TRY(scratch(P, 3, S));
     double2 *bc = plan_bc(P, 0), *coef = plan_bc(P, 1);
     if (!bc || !coef) { set_error("out of device memory"); return ERR_OOM; }
-    k_poisson<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a), F<T>(b), F<T>(c), F<T>(d), F<T>(S[0]), bctarget);
+    { Launch L_(P, "poisson", 8.0 * cplx_rows(P, P.nz)); k_poisson<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a), F<T>(b), F<T>(c), F<T>(d), F<T>(S[0]), bctarget); }
     SG_TRY(check_launch("poisson"));
     SG_TRY(wall_eval<T>(P, S[0], 1.0, bc, bctarget == 0));
-    k_laplace_coef<<<dim3(cdiv(P.nxh, 64), P.ny), 64, 0, P.stream>>>(P.geo, bc, coef, bctarget);
+    { Launch L_(P, "laplace_coef", 64.0 * P.nxh * P.ny); k_laplace_coef<<<dim3(cdiv(P.nxh, 64), P.ny), 64, 0, P.stream>>>(P.geo, bc, coef, bctarget); }
     SG_TRY(check_launch("laplace_coef"));
-    k_laplace_profile<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, coef, F<T>(S[1]), F<T>(S[2]));
+    { Launch L_(P, "laplace_profile", 2.0 * cplx_rows(P, P.nz)); k_laplace_profile<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, coef, F<T>(S[1]), F<T>(S[2])); }
     SG_TRY(check_launch("laplace_profile"));
     ZInvArgs z{};
     if (bctarget == 0) {
@@ -494,7 +539,7 @@ template <typename T> int Ops<T>::sol_project(Plan &P, void *a, void *b, void *c
     ZFwdArgs f{};
     f.in[0] = S[1]; f.out[0] = S[1]; f.in[1] = S[2]; f.out[1] = S[2]; f.in_scale = 1.0;
     SG_TRY(launch_z_forward<T>(P, f, 2));
-    k_proj_sub<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a), F<T>(b), F<T>(c), F<T>(S[1]), F<T>(S[2]));
+    { Launch L_(P, "proj_sub", 8.0 * cplx_rows(P, P.nz)); k_proj_sub<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(a), F<T>(b), F<T>(c), F<T>(S[1]), F<T>(S[2])); }
     return check_launch("proj_sub");
 }
 
@@ -513,7 +558,7 @@ int Ops<T>::v_imposebc_and_project(Plan &P, void *vx, void *vy, void *vz, void *
     double tmp = 1 / (double)rki;
     if (rki != ord) tmp = (double)(rki + 1) * tmp;
     WallVel vb{vzsta[0], vzsta[1], vzend[0], vzend[1]};
-    k_noslip<T><<<dim3(cdiv(P.nxh, 64), P.ny), 64, 0, P.stream>>>(P.geo, F<T>(vx), F<T>(vy), F<T>(pr), tmp, vb);
+    { Launch L_(P, "noslip", cplx_rows(P, 6)); k_noslip<T><<<dim3(cdiv(P.nxh, 64), P.ny), 64, 0, P.stream>>>(P.geo, F<T>(vx), F<T>(vy), F<T>(pr), tmp, vb); }
     SG_TRY(check_launch("noslip"));
     // goto_3d_fourier (boundary_mod.fpp:153-194)
     ZFwdArgs f{};
@@ -528,7 +573,7 @@ template <typename T> int Ops<T>::s_imposebc(Plan &P, void *th) {
     z.in[0] = th; z.out0[0] = th;
     z.nrows = P.nzp; z.scale_rows = P.nzp; z.scale = 1.0 / (double)P.nz;
     SG_TRY(launch_z_inverse<T>(P, z, 1));
-    k_zero_walls<T><<<dim3(cdiv(P.nxh, 64), P.ny), 64, 0, P.stream>>>(P.geo, F<T>(th));
+    { Launch L_(P, "zero_walls", cplx_rows(P, 2)); k_zero_walls<T><<<dim3(cdiv(P.nxh, 64), P.ny), 64, 0, P.stream>>>(P.geo, F<T>(th)); }
     SG_TRY(check_launch("zero_walls"));
     return fftp1d_r2c_z(P, th);
 }
@@ -536,12 +581,12 @@ template <typename T> int Ops<T>::s_imposebc(Plan &P, void *th) {
 // ------------------------------------------------------------------------- stage
 
 template <typename T> int Ops<T>::axpy_sub(Plan &P, void *y, const void *x, double s) {
-    k_sub_scaled<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(y), F<T>(x), s);
+    { Launch L_(P, "sub_scaled", 3.0 * cplx_rows(P, P.nz)); k_sub_scaled<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(y), F<T>(x), s); }
     return check_launch("sub_scaled");
 }
 
 template <typename T> int Ops<T>::rk_update(Plan &P, void *v, const void *Cold, const void *N, double dt, double nu, double rmp) {
-    k_rk_update<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(v), F<T>(Cold), F<T>(N), dt, nu, rmp);
+    { Launch L_(P, "rk_update", 4.0 * cplx_rows(P, P.nz)); k_rk_update<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(P.geo, F<T>(v), F<T>(Cold), F<T>(N), dt, nu, rmp); }
     return check_launch("rk_update");
 }
 
@@ -551,7 +596,7 @@ static __global__ void k_scale_real(T *r, long long n, T s) {
 }
 
 template <typename T> int Ops<T>::scale_real(Plan &P, void *r, double s) {
-    k_scale_real<T><<<152 * 8, kThreads, 0, P.stream>>>((T *)r, (long long)P.real_elems(), (T)s);
+    { Launch L_(P, "scale_real", 2.0 * P.real_elems() * P.rel()); k_scale_real<T><<<152 * 8, kThreads, 0, P.stream>>>((T *)r, (long long)P.real_elems(), (T)s); }
     return check_launch("scale_real");
 }
 

@@ -213,6 +213,11 @@ int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], cons
         plan_destroy(p);
         return st;
     }
+    if (p->prec == FP32 && ((st = build_fft4_table(p->tx4, p->H)) || (st = build_fft4_table(p->ty4, ny)) ||
+                            (st = build_fft4_table(p->tz4, nz)))) {
+        plan_destroy(p);
+        return st;
+    }
     cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
     Geo &G = p->geo;
     G.nx = nx; G.ny = ny; G.nz = nz; G.cz = p->cz; G.oz = p->oz; G.nxh = p->nxh; G.nzp = p->nzp;
@@ -231,6 +236,7 @@ int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], cons
         }
         cudaMalloc(&p->dwtw, w.size() * sizeof(double));
         cudaMemcpy(p->dwtw, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice);
+        G.wtw = p->dwtw;
     }
     cudaMallocHost(&p->hred, sizeof(double) * 64);
     if (cudaGetLastError() != cudaSuccess) { set_error("CUDA error during plan creation"); plan_destroy(p); return ERR_CUDA; }
@@ -248,11 +254,57 @@ void *Plan::scratch_field(int i) {
     return scratch[i];
 }
 
+static cudaEvent_t take_event(Plan *p) {
+    if (!p->evpool.empty()) {
+        cudaEvent_t e = p->evpool.back();
+        p->evpool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void Plan::prof_begin(const char *name, double bytes) {
+    launches++;
+    if (!profile) return;
+    Rec r{name, bytes, take_event(this), take_event(this)};
+    cudaEventRecord(r.a, stream);
+    recs.push_back(r);
+}
+
+void Plan::prof_end() {
+    if (!profile || recs.empty()) return;
+    cudaEventRecord(recs.back().b, stream);
+    if (recs.size() >= 4096) prof_flush();
+}
+
+void Plan::prof_flush() {
+    if (recs.empty()) return;
+    cudaStreamSynchronize(stream);
+    for (Rec &r : recs) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, r.a, r.b);
+        bool found = false;
+        for (Agg &g : agg)
+            if (g.name == r.name) { g.n++; g.ms += ms; g.bytes += r.bytes; found = true; break; }
+        if (!found) agg.push_back(Agg{r.name, 1, (double)ms, r.bytes});
+        timers[4] += ms * 1e-3;
+        if (strncmp(r.name, "layout", 6) == 0) timers[1] += ms * 1e-3; else timers[0] += ms * 1e-3;
+        evpool.push_back(r.a);
+        evpool.push_back(r.b);
+    }
+    recs.clear();
+}
+
 void plan_destroy(Plan *p) {
     if (!p) return;
     if (p->stream) cudaStreamSynchronize(p->stream);
+    p->prof_flush();
+    for (cudaEvent_t e : p->evpool) cudaEventDestroy(e);
     for (void *m : p->scratch) cudaFree(m);
     free_fft_table(p->tx); free_fft_table(p->ty); free_fft_table(p->tz);
+    free_fft4_table(p->tx4); free_fft4_table(p->ty4); free_fft4_table(p->tz4);
     if (p->dgeo) cudaFree(p->dgeo);
     if (p->dxtw) cudaFree(p->dxtw);
     if (p->dred) cudaFree(p->dred);

@@ -25,12 +25,25 @@ struct FFTTable {
     void *mem = nullptr;  // one device allocation holding tw / chirp / filters
 };
 
+// tables of the register four-step engine (fft4.cuh) for one axis; ok == 0 when the axis
+// length has no compiled four-step kernel and the generic engine is used
+struct FFT4Desc {
+    int n, L, L1, L2, blue;
+    const void *tw4, *chirp, *filtf, *filtb;
+};
+struct FFT4Table {
+    FFT4Desc d{};
+    void *mem = nullptr;
+    int ok = 0;
+};
+
 // Geometry passed to kernels by value.
 struct Geo {
     int nx, ny, nz, cz, oz, nxh, nzp, ldx, H;
     const double *kx, *ky, *kz, *z, *dir;     // device, FP64
     const double *fx, *fy, *fz;               // fc_filter factors per axis (FP64)
     const void *xtw;                          // C2<T>[H+1]: exp(-2*pi*i*k/nx)
+    const void *wtw;                          // double2[nz]: exp(+2*pi*i*k*(nzp-1)/nz)
     double Lz;
 };
 
@@ -42,6 +55,7 @@ struct Plan {
     double *dgeo = nullptr;   // device block holding kx, ky, kz, z, dir, fx, fy, fz
     void *dxtw = nullptr;
     FFTTable tx, ty, tz;      // lengths H = nx/2, ny, nz
+    FFT4Table tx4, ty4, tz4;  // four-step tables of the same lengths (FP32 plans)
     cudaStream_t stream = nullptr;
     Geo geo{};
     // scratch (lazily allocated, complex fields / small buffers)
@@ -50,9 +64,21 @@ struct Plan {
     double *dwtw = nullptr;   // exp(+2 pi i k (nzp-1)/nz), k < nz: inverse-z twiddles at the top wall
     double *hred = nullptr;   // pinned host mirror
     int nred = 0;
-    // per-phase timers (ms), mirroring the reference's ffttime/tratime/comtime/conttime/tottime
+    // per-phase timers (s), mirroring the reference's ffttime/tratime/comtime/conttime/tottime
     double timers[6] = {0, 0, 0, 0, 0, 0};
+    // kernel accounting: launches counted always; with profiling on, every launch is bracketed
+    // by CUDA events on the plan stream and attributed to its kernel name with its
+    // algorithmic bytes (compulsory reads + writes of that launch)
+    long long launches = 0;
     bool profile = false;
+    struct Rec { const char *name; double bytes; cudaEvent_t a, b; };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> evpool;
+    struct Agg { std::string name; long long n; double ms, bytes; };
+    std::vector<Agg> agg;
+    void prof_begin(const char *name, double bytes);
+    void prof_end();
+    void prof_flush();
 
     size_t elt() const { return prec == FP64 ? 16 : 8; }                // bytes per complex element
     size_t rel() const { return prec == FP64 ? 8 : 4; }                 // bytes per real element
@@ -67,5 +93,7 @@ int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], cons
 void plan_destroy(Plan *p);
 int build_fft_table(FFTTable &t, int n, Prec prec);
 void free_fft_table(FFTTable &t);
+int build_fft4_table(FFT4Table &t, int n);  // fast_f32.cu
+void free_fft4_table(FFT4Table &t);
 
 }  // namespace sg
