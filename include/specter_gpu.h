@@ -110,6 +110,16 @@ int specter_product(specter_plan *plan, const specter_field *a, const specter_fi
 /* ---- boundary (src/boundary/boundary_mod.fpp, vboundary.f90, sboundary.f90) */
 int specter_bouncheck_z(specter_plan *plan, const specter_field *a, const specter_field *b,
                         double *bot, double *top);                                                   /* boundary_mod :681-801 (b may be NULL) */
+/* Same result as specter_bouncheck_z, computed without allocating any memory.  It has no
+ * counterpart in the reference.  For callers that may not allocate once they are running: a
+ * serving loop that has committed its device memory budget, or code in the middle of the RK
+ * loop that cannot take the device-wide synchronisation of cudaMalloc/cudaFree.  Its working
+ * memory is one fixed device array (4 MiB, held on every GPU that loads the library until
+ * exit): grids with more than 65536 (kx, ky) columns are rejected with SPECTER_ERR_SHAPE.
+ * All calls share that array, so calls that overlap on the GPU race; the first call on a
+ * device looks up the array's address and should come before any stream capture. */
+int specter_bouncheck_z_static(specter_plan *plan, const specter_field *a, const specter_field *b,
+                               double *bot, double *top);
 int specter_sol_project(specter_plan *plan, specter_field *a, specter_field *b, specter_field *c,
                         specter_field *d, int bctarget, int bczsta, int bczend);                     /* boundary_mod :197-402 */
 int specter_v_imposebc_and_project(specter_plan *plan, specter_field *vx, specter_field *vy,

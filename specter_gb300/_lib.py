@@ -27,7 +27,8 @@ EXPORTS = [
     "specter_derivk", "specter_laplak", "specter_curlk", "specter_gradre", "specter_advect",
     "specter_fc_filter", "specter_energy", "specter_helicity", "specter_cross", "specter_divergence",
     "specter_variance", "specter_product",
-    "specter_bouncheck_z", "specter_sol_project", "specter_v_imposebc_and_project", "specter_s_imposebc",
+    "specter_bouncheck_z", "specter_bouncheck_z_static", "specter_sol_project", "specter_v_imposebc_and_project",
+    "specter_s_imposebc",
     "specter_solver_create", "specter_solver_destroy", "specter_solver_fields", "specter_solver_step",
     "specter_solver_stage", "specter_solver_check",
     "specter_timers", "specter_timers_reset",
@@ -74,6 +75,7 @@ def load(path: str | None = None):
     L.specter_variance.argtypes = [VP, VP, C.c_int, PD]
     L.specter_product.argtypes = [VP, VP, VP, PD]
     L.specter_bouncheck_z.argtypes = [VP, VP, VP, PD, PD]
+    L.specter_bouncheck_z_static.argtypes = [VP, VP, VP, PD, PD]
     L.specter_sol_project.argtypes = [VP] * 5 + [C.c_int] * 3
     L.specter_v_imposebc_and_project.argtypes = [VP] * 5 + [C.c_int, C.c_int, PD, PD]
     L.specter_derivk.argtypes = [VP, VP, VP, C.c_int]

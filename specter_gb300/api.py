@@ -282,6 +282,13 @@ def bouncheck_z(plan, a, b=None):
     return bot.value, top.value
 
 
+def bouncheck_z_static(plan, a, b=None):
+    """bouncheck_z without allocating: working memory is a fixed device array (see the C header)."""
+    bot, top = C.c_double(), C.c_double()
+    check(_L(plan).specter_bouncheck_z_static(plan.h, a.h, b.h if b is not None else None, C.byref(bot), C.byref(top)))
+    return bot.value, top.value
+
+
 def sol_project(plan, a, b, c, d, bctarget=1, bczsta=0, bczend=0):
     check(_L(plan).specter_sol_project(plan.h, a.h, b.h, c.h, d.h, bctarget, bczsta, bczend))
 
