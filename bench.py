@@ -186,6 +186,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--refseq", action="store_true", help="time the reference call sequence instead of the fused stages")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--grid", default=None, help="NX,NY,NZP: another grid of the same case (profiling, sweeps)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -203,7 +204,10 @@ def main():
     api.set_device(local)
     K, W = args.steps, max(args.warmup, 3)
 
-    plan, s = build_solver(api, initial, CFG, api.FP32, fused=not args.refseq)
+    cfg = dict(CFG)
+    if args.grid:
+        cfg["nx"], cfg["ny"], cfg["nzp"] = (int(v) for v in args.grid.split(","))
+    plan, s = build_solver(api, initial, cfg, api.FP32, fused=not args.refseq)
     stream = torch.cuda.ExternalStream(plan.stream, device=torch.device("cuda", local))
     for _ in range(W):
         s.step(1)
@@ -230,8 +234,8 @@ def main():
     if dist:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     ms = float(t.item())
-    pts = CFG["nx"] * CFG["ny"] * CFG["nzp"]
-    value = world * pts * CFG["ord"] * K / (ms * 1e-3) / 1e6
+    pts = cfg["nx"] * cfg["ny"] * cfg["nzp"]
+    value = world * pts * cfg["ord"] * K / (ms * 1e-3) / 1e6
 
     # end to end: state uploaded from pinned host memory and downloaded every step
     fields = [f for f in (s.vx, s.vy, s.vz, s.th, s.pr)]
@@ -254,23 +258,25 @@ def main():
     te_t = torch.tensor([te], device=f"cuda:{local}")
     if dist:
         dist.all_reduce(te_t, op=dist.ReduceOp.MAX)
-    e2e = world * pts * CFG["ord"] * Ke / float(te_t.item()) / 1e6
+    e2e = world * pts * cfg["ord"] * Ke / float(te_t.item()) / 1e6
     nbytes = sum(f.nbytes for f in fields)
 
     if rank == 0:
+        field_mb = (cfg["nx"] // 2 + 1) * cfg["ny"] * (cfg["nzp"] + cfg["cz"]) * 8 / 1e6
         peak, peak_kind = peaks()
         roof = dominant_roofline(report, peak, load_traffic())
         roof["peak_kind"] = peak_kind
         # stage-level model of the frozen measurement definition: B = 128 * N * s per BOUSS stage
-        N = CFG["nx"] * CFG["ny"] * (CFG["nzp"] + CFG["cz"])
-        model_gbs = 128 * N * 4 * CFG["ord"] * K / (ms * 1e-3) / 1e9
+        N = cfg["nx"] * cfg["ny"] * (cfg["nzp"] + cfg["cz"])
+        model_gbs = 128 * N * 4 * cfg["ord"] * K / (ms * 1e-3) / 1e9
         line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": K,
                 "warmup": W, "ms_per_step": round(ms / K, 4), "higher_is_better": True,
                 "scaling": "weak" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic",
-                "config": {"workload": "BOUSS Rayleigh-Benard 512x512x513 (+25 FC-Gram, NZ=538), FP32-bulk, RK2, dt=1e-5",
+                "config": {"workload": f"BOUSS Rayleigh-Benard {cfg['nx']}x{cfg['ny']}x{cfg['nzp']} (+{cfg['cz']} FC-Gram, "
+                                       f"NZ={cfg['nzp'] + cfg['cz']}), FP32-bulk, RK2, dt=1e-5",
                            "path": "reference-sequence" if args.refseq else "fused",
-                           "l2": "inputs larger than L2 (566 MB per field), no flush",
+                           "l2": f"inputs larger than L2 ({field_mb:.0f} MB per field), no flush",
                            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
                 "roofline": roof,
                 "stage_model": {"bytes_per_stage": 128 * N * 4, "achieved_gbs": round(model_gbs, 1),

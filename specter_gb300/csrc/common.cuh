@@ -34,4 +34,45 @@ template <typename V> __device__ __forceinline__ V cmuli(V a, int s) {
 
 __host__ __device__ __forceinline__ int cdiv(int a, int b) { return (a + b - 1) / b; }
 
+// ---- asynchronous global -> shared copies (cp.async): the copies of a whole tile are in
+// flight together; async_wait() completes them for the calling thread (a barrier follows).
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem_dst, const void *gmem_src) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    if constexpr (BYTES == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem_src), "n"(BYTES) : "memory");
+}
+__device__ __forceinline__ void async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void async_wait() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+// wait until at most N of the calling thread's most recent copy groups are still in flight
+template <int N>
+__device__ __forceinline__ void async_wait_n() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Asynchronously copy a [rows][TK] complex column tile: element (k, c) comes from
+// src[k*stride + c] for c < nv and is zero for nv <= c < TK.  Call async_wait() and
+// __syncthreads() before reading the tile.
+template <typename V>
+__device__ __forceinline__ void tile_load_async(V *dst, const V *src, size_t stride, int rows, int TK, int nv) {
+    for (int idx = threadIdx.x; idx < rows * TK; idx += blockDim.x) {
+        const int k = idx / TK, c = idx % TK;
+        if (c < nv) cp_async<sizeof(V)>(dst + idx, src + (size_t)k * stride + c);
+        else { V z; z.x = 0; z.y = 0; dst[idx] = z; }
+    }
+    async_commit();
+}
+
+// Same for rows stored contiguously: element (k, c) of the [rows][TK] tile comes from
+// src[c*cstride + k] (c < nv), so consecutive threads read consecutive k.
+template <typename V>
+__device__ __forceinline__ void rows_load_async(V *dst, const V *src, size_t cstride, int rows, int TK, int nv) {
+    for (int idx = threadIdx.x; idx < rows * TK; idx += blockDim.x) {
+        const int c = idx / rows, k = idx % rows;
+        if (c < nv) cp_async<sizeof(V)>(dst + k * TK + c, src + (size_t)c * cstride + k);
+        else { V z; z.x = 0; z.y = 0; dst[k * TK + c] = z; }
+    }
+    async_commit();
+}
+
 }  // namespace sg

@@ -133,10 +133,14 @@ int done(const char *what) {
 }
 
 template <int L1, int L2>
-int zinv(Plan &P, const ZInvArgs &a, int nf, double bytes) {
+int zinv(Plan &P, const ZInvArgs &a0, int nf, double bytes) {
     using E = FourStep<float, L1, L2>;
-    const int tk = pick((size_t)P.tz4.d.L * sizeof(float2));
-    const size_t sm = (size_t)P.tz4.d.L * tk * sizeof(float2);
+    ZInvArgs a = a0;
+    a.staged = 0;
+    for (int f = 0; f < nf; f++) a.staged |= (a.out0[f] && a.out1[f]) ? 1 : 0;
+    const size_t per = ((size_t)P.tz4.d.L + (a.staged ? P.nz : 0)) * sizeof(float2);
+    const int tk = pick(per);
+    const size_t sm = per * tk;
     smem_attr(k_z_inverse<float, E>, sm);
     Scope s(P, "z_inverse", bytes);
     k_z_inverse<float, E><<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz4.d, a, tk);
@@ -155,10 +159,14 @@ int zfwd(Plan &P, const ZFwdArgs &a, int nf, double bytes) {
 }
 
 template <int L1, int L2>
-int ypass(Plan &P, const YArgs &a, int nf, int nplanes, double bytes) {
+int ypass(Plan &P, const YArgs &a0, int nf, int nplanes, double bytes) {
     using E = FourStep<float, L1, L2>;
-    const int tk = pick((size_t)P.ty4.d.L * sizeof(float2));
-    const size_t sm = (size_t)P.ty4.d.L * tk * sizeof(float2);
+    YArgs a = a0;
+    a.staged = 0;
+    for (int f = 0; f < nf; f++) a.staged |= (a.out0[f] && a.out1[f]) ? 1 : 0;
+    const size_t per = ((size_t)P.ty4.d.L + (a.staged ? P.ny : 0)) * sizeof(float2);
+    const int tk = pick(per);
+    const size_t sm = per * tk;
     smem_attr(k_y_pass<float, E>, sm);
     Scope s(P, a.sign < 0 ? "y_forward" : "y_inverse", bytes);
     k_y_pass<float, E><<<dim3(cdiv(P.nxh, tk), nplanes, nf), kThreads, sm, P.stream>>>(P.geo, P.ty4.d, a, tk);
@@ -187,7 +195,7 @@ int xpass(Plan &P, const XArgs &a, int nf, bool r2c, double bytes) {
 template <int L1, int L2>
 int xnl(Plan &P, const XNLArgs &a, double bytes) {
     using E = FourStep<float, L1, L2>;
-    const size_t per = ((size_t)P.tx4.d.L + P.nxh + (4 + (a.c1 - a.c0)) * (size_t)P.H) * sizeof(float2);
+    const size_t per = ((size_t)P.tx4.d.L + 2 * (size_t)P.nxh + (4 + (a.c1 - a.c0)) * (size_t)P.H) * sizeof(float2);
     const int rb = pick(per, 200 * 1024);
     if (!rb) return kNoFast;
     const size_t sm = per * rb;

@@ -55,23 +55,46 @@ __device__ __forceinline__ void fc_continuation_fn(const Geo &g, C2<T> *X, int T
     }
 }
 
-// laplace_z profile of column (kx, ky) at grid point zz (boundary_mod.fpp:635-675): a and b = da/dz.
-// EXP = double evaluates the exponentials in FP64; EXP = float in FP32 (the bulk rows of the
-// FP32 form, which are rounded to FP32 for the transform anyway).  Coefficients are FP64.
-template <typename EXP>
-__device__ __forceinline__ void lap_profile(const Geo &g, int kx, int ky, double2 c1, double2 c2, double zz,
-                                            double2 &a, double2 &b) {
+// laplace_z profile of column (kx, ky) at grid point zz (boundary_mod.fpp:635-675), FP64:
+// a and b = da/dz.  Used for the 2d rows that feed the FC-Gram continuation.
+__device__ __forceinline__ void lap_profile_d(const Geo &g, int kx, int ky, double2 c1, double2 c2, double zz,
+                                              double2 &a, double2 &b) {
     if (kx == 0 && ky == 0) {
         a = make_double2(c1.x * zz + c2.x, 0.0);
         b = make_double2(c1.x, 0.0);
     } else {
         const double kh = sqrt(g.kx[kx] * g.kx[kx] + g.ky[ky] * g.ky[ky]);
-        double e1, e2;
-        if constexpr (sizeof(EXP) == 8) { e1 = exp(kh * (zz - g.Lz)); e2 = exp(-(kh * zz)); }
-        else { e1 = (double)expf((float)(kh * (zz - g.Lz))); e2 = (double)expf((float)(-(kh * zz))); }
+        const double e1 = exp(kh * (zz - g.Lz)), e2 = exp(-(kh * zz));
         a = make_double2(c1.x * e1 + c2.x * e2, c1.y * e1 + c2.y * e2);
         b = make_double2(kh * (c1.x * e1 - c2.x * e2), kh * (c1.y * e1 - c2.y * e2));
     }
+}
+
+// Per-column laplace_z parameters in the kernel's precision: kh = |(kx, ky)| and the
+// coefficients c1, c2 (solved in FP64, then rounded); k0 marks the (0, 0) column.
+template <typename T>
+struct LapCol {
+    T kh;
+    C2<T> c1, c2;
+    int k0;
+};
+
+template <typename T> __device__ __forceinline__ T exp_t(T x);
+template <> __device__ __forceinline__ float exp_t<float>(float x) { return expf(x); }
+template <> __device__ __forceinline__ double exp_t<double>(double x) { return exp(x); }
+
+// The same profile on the bulk rows, in the kernel's precision (they enter the z transform
+// in that precision).
+template <typename T>
+__device__ __forceinline__ void lap_profile_t(const LapCol<T> &p, T zz, T Lz, C2<T> &a, C2<T> &b) {
+    if (p.k0) {
+        a = mk<T>(p.c1.x * zz + p.c2.x, (T)0);
+        b = mk<T>(p.c1.x, (T)0);
+        return;
+    }
+    const T e1 = exp_t<T>(p.kh * (zz - Lz)), e2 = exp_t<T>(-(p.kh * zz));
+    a = mk<T>(p.c1.x * e1 + p.c2.x * e2, p.c1.y * e1 + p.c2.y * e2);
+    b = mk<T>(p.kh * (p.c1.x * e1 - p.c2.x * e2), p.kh * (p.c1.y * e1 - p.c2.y * e2));
 }
 
 // Neumann laplace_z coefficients from the wall values (boundary_mod.fpp:521-549), FP64
@@ -110,33 +133,66 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
     auto colq = [&](int z, int c) { return fidx<T>(g, z, ky, kx0 + c); };
     const T dt = (T)a.dt, nu = (T)a.nu, rmp = (T)a.rmp;
 
-    // ---- 1. NL forward transforms, buoyancy, filter, laplak, RK update -> U[c]
+    // ---- 1. NL forward transforms, buoyancy, filter, laplak, RK update -> U[c].  Every HBM
+    //         read is an asynchronous tile copy: NL_{c+1} (or theta, for the buoyancy of
+    //         c = z) goes into the still unused slot U[c+1] while component c is transformed;
+    //         vin and cold go into the FFT buffer once the transformed NL has been consumed.
+    const size_t tile = (size_t)nz * TK;
+    const size_t zs = (size_t)g.ny * g.ldx, col0 = (size_t)ky * g.ldx + kx0;
+    const bool stage2 = (size_t)E::kBuffers * L >= 2 * (size_t)nz;  // vin and cold both fit
     for (int c3 = 0; c3 < 3; c3++) {
-        const V *nl = (const V *)a.nl[c3];
-        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
-            X[idx] = c < nv ? nl[colq(k, c)] : mk<T>(0, 0);
+        V *Uc = U + c3 * tile;
+        const bool buoy = c3 == 2 && a.bouss;
+        if (c3 == 0) {
+            tile_load_async(X, (const V *)a.nl[0] + col0, zs, nzp, TK, nv);
+            tile_load_async(U + tile, (const V *)a.nl[1] + col0, zs, nzp, TK, nv);
+            async_wait_n<1>();
+        } else {
+            async_wait();
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Uc[idx];
+            __syncthreads();
+            if (c3 == 1) tile_load_async(U + 2 * tile, (const V *)a.nl[2] + col0, zs, nzp, TK, nv);
+            else if (buoy) tile_load_async(Uc, (const V *)a.vin[3] + col0, zs, nz, TK, nv);
         }
         __syncthreads();
         fc_continuation<T>(g, X, TK);
         __syncthreads();
         V *R = E::run(X, Y, TK, fd, -1);
-        const V *vin = (const V *)a.vin[c3], *cold = (const V *)a.cold[c3];
-        const V *th = (const V *)a.vin[3];
+        if (buoy) {
+            async_wait();
+            __syncthreads();
+        }
+        // (a) filtered nonlinear term (minus buoyancy) -> U[c]
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
             const int k = idx / TK, c = idx % TK;
-            if (c >= nv) { U[(size_t)c3 * nz * TK + idx] = mk<T>(0, 0); continue; }
+            V n = mk<T>(0, 0);
+            if (c < nv) {
+                const int kx = kx0 + c;
+                n = R[E::pos(k, fd) * TK + c];
+                if (buoy) { const V t = Uc[idx]; n = mk<T>(n.x - (T)a.xmom * t.x, n.y - (T)a.xmom * t.y); }
+                n = cscale(n, g.FX<T>(kx));
+                n = cscale(n, g.FY<T>(ky));
+                n = cscale(n, g.FZ<T>(k));
+            }
+            Uc[idx] = n;
+        }
+        __syncthreads();
+        // (b) RK update with laplak of the stage input
+        const V *cold = (const V *)a.cold[c3];
+        tile_load_async(X, (const V *)a.vin[c3] + col0, zs, nz, TK, nv);
+        if (stage2) tile_load_async(X + tile, cold + col0, zs, nz, TK, nv);
+        async_wait();
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            if (c >= nv) { Uc[idx] = mk<T>(0, 0); continue; }
             const int kx = kx0 + c;
-            const size_t q = colq(k, c);
-            V n = R[E::pos(k, fd) * TK + c];
-            if (c3 == 2 && a.bouss) { const V t = th[q]; n = mk<T>(n.x - (T)a.xmom * t.x, n.y - (T)a.xmom * t.y); }
-            n = cscale(n, (T)g.fx[kx]);
-            n = cscale(n, (T)g.fy[ky]);
-            n = cscale(n, (T)g.fz[k]);
-            const T k2 = (T)g.kx[kx] * (T)g.kx[kx] + (T)g.ky[ky] * (T)g.ky[ky] + (T)g.kz[k] * (T)g.kz[k];
-            const V v = vin[q], cv = cold[q];
+            const T k2 = g.KX<T>(kx) * g.KX<T>(kx) + g.KY<T>(ky) * g.KY<T>(ky) + g.KZ<T>(k) * g.KZ<T>(k);
+            const V v = X[idx], cv = stage2 ? X[tile + idx] : cold[colq(k, c)];
+            const V n = Uc[idx];
             const V lap = cscale(v, -k2);
-            U[(size_t)c3 * nz * TK + idx] = mk<T>(cv.x + dt * (nu * lap.x - n.x) * rmp, cv.y + dt * (nu * lap.y - n.y) * rmp);
+            Uc[idx] = mk<T>(cv.x + dt * (nu * lap.x - n.x) * rmp, cv.y + dt * (nu * lap.y - n.y) * rmp);
         }
         __syncthreads();
     }
@@ -154,7 +210,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
             if ((k == 0 || k == nzp - 1) && c < nv) {
                 const int kx = kx0 + c;
                 const V p = pr[colq(k, c)];
-                v = cscale(cimk((T)(c3 == 0 ? g.kx[kx] : g.ky[ky]), p), (T)a.wall_tmp);
+                v = cscale(cimk(c3 == 0 ? g.KX<T>(kx) : g.KY<T>(ky), p), (T)a.wall_tmp);
                 if (kx == 0 && ky == 0) v = mk<T>((T)((double)g.nx * g.ny * a.vb[(k == 0 ? 0 : 2) + c3]), (T)0);
             }
             Uc[idx] = v;  // physical rows, natural order (temporary)
@@ -171,27 +227,31 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
         }
         __syncthreads();
     }
-    // ---- 3. poisson_inhomogeneous: d -> X (natural), v -= i k d, wall sums of vz/nz (FP64)
+    // ---- 3. poisson_inhomogeneous: d -> X (natural), v -= i k d, wall sums of vz (FP64)
     const double2 *wtw = (const double2 *)g.wtw;
+    double2 *bnd = coef + 2 * TK;                                 // [TK][2][2d] FP64 profile rows
+    LapCol<T> *lcol = (LapCol<T> *)(bnd + (size_t)TK * 4 * g.oz);  // [TK]
+    const int d = g.oz;
     {
         const int c = threadIdx.x % TK, k0 = threadIdx.x / TK, kstep = blockDim.x / TK;
+        const int kxc = min(kx0 + c, g.nxh - 1);
+        const T kx_ = g.KX<T>(kxc), ky_ = g.KY<T>(ky);
         double2 s0 = make_double2(0, 0), s1 = make_double2(0, 0);
         if (threadIdx.x < kstep * TK) {
             for (int k = k0; k < nz; k += kstep) {
                 const int idx = k * TK + c;
-                const int kx = kx0 + c;
-                const T kx_ = (T)g.kx[min(kx, g.nxh - 1)], ky_ = (T)g.ky[ky], kz_ = (T)g.kz[k];
+                const T kz_ = g.KZ<T>(k);
                 const T k2 = kx_ * kx_ + ky_ * ky_ + kz_ * kz_;
                 V A = U[idx], B = U[(size_t)nz * TK + idx], Cc = U[(size_t)2 * nz * TK + idx];
                 const V s = mk<T>(kx_ * A.x + ky_ * B.x + kz_ * Cc.x, kx_ * A.y + ky_ * B.y + kz_ * Cc.y);
                 V D = mk<T>(s.y / k2, -s.x / k2);
-                if (k == 0 && ky == 0 && kx == 0) D = mk<T>(0, 0);
+                if (k == 0 && ky == 0 && kx0 + c == 0) D = mk<T>(0, 0);
                 A = csub(A, cimk(kx_, D));
                 B = csub(B, cimk(ky_, D));
                 Cc = csub(Cc, cimk(kz_, D));
                 U[idx] = A; U[(size_t)nz * TK + idx] = B; U[(size_t)2 * nz * TK + idx] = Cc;
                 X[idx] = D;
-                const double vr = (double)Cc.x / nz, vi = (double)Cc.y / nz;
+                const double vr = (double)Cc.x, vi = (double)Cc.y;
                 const double2 w = wtw[k];
                 s0.x += vr; s0.y += vi;
                 s1.x += vr * w.x - vi * w.y;
@@ -209,49 +269,58 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
             const double2 p0 = red[2 * (t * TK + c)], p1 = red[2 * (t * TK + c) + 1];
             b1.x += p0.x; b1.y += p0.y; b2.x += p1.x; b2.y += p1.y;
         }
+        const double inz = 1.0 / nz;  // wall values of vz / nz
+        b1.x *= inz; b1.y *= inz; b2.x *= inz; b2.y *= inz;
+        const int kxc = min(kx0 + c, g.nxh - 1);
         double2 c1, c2;
-        lap_coef_neumann(g, min(kx0 + c, g.nxh - 1), ky, b1, b2, c1, c2);
+        lap_coef_neumann(g, kxc, ky, b1, b2, c1, c2);
         coef[2 * c] = c1;
         coef[2 * c + 1] = c2;
+        LapCol<T> lc;
+        lc.kh = (T)sqrt(g.kx[kxc] * g.kx[kxc] + g.ky[ky] * g.ky[ky]);
+        lc.c1 = mk<T>((T)c1.x, (T)c1.y);
+        lc.c2 = mk<T>((T)c2.x, (T)c2.y);
+        lc.k0 = kxc == 0 && ky == 0;
+        lcol[c] = lc;
     }
     __syncthreads();
-    // ---- 4. pressure: pr = IFFT_z(d)/nz + a(z) on the physical rows
+    // ---- 4. pressure: pr = IFFT_z(d)/nz + a(z) on the physical rows; FP64 a, b on the 2d
+    //         rows that feed the continuation of step 5
     {
-        V *R = E::run(X, Y, TK, fd, +1);
-        V *prw = (V *)a.pr;
-        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
-            if (c >= nv) continue;
-            double2 pa, pb;
-            lap_profile<T>(g, kx0 + c, ky, coef[2 * c], coef[2 * c + 1], g.z[k], pa, pb);
-            const V dv = R[E::pos(k, fd) * TK + c];
-            const T inz = (T)1 / (T)nz;
-            prw[colq(k, c)] = mk<T>((T)((double)(dv.x * inz) + pa.x), (T)((double)(dv.y * inz) + pa.y));
-        }
-        __syncthreads();
-    }
-    // ---- 5. harmonic correction: a and b profiles; the 2d rows that feed the FC-Gram
-    //         continuation are evaluated and continued in FP64, then forward transformed
-    double2 *bnd = coef + 2 * TK;  // [TK][2d]: rows 0..d-1 then nzp-d..nzp-1
-    const int d = g.oz;
-    for (int which = 0; which < 2; which++) {
-        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
-            double2 pa, pb;
-            lap_profile<T>(g, min(kx0 + c, g.nxh - 1), ky, coef[2 * c], coef[2 * c + 1], g.z[k], pa, pb);
-            const double2 p = which == 0 ? pa : pb;
-            X[idx] = mk<T>((T)p.x, (T)p.y);
-        }
         for (int idx = threadIdx.x; idx < 2 * d * TK; idx += blockDim.x) {
             const int j = idx / TK, c = idx % TK;
             const int row = j < d ? j : nzp - 2 * d + j;
             double2 pa, pb;
-            lap_profile<double>(g, min(kx0 + c, g.nxh - 1), ky, coef[2 * c], coef[2 * c + 1], g.z[row], pa, pb);
-            bnd[c * 2 * d + j] = which == 0 ? pa : pb;
+            lap_profile_d(g, min(kx0 + c, g.nxh - 1), ky, coef[2 * c], coef[2 * c + 1], g.z[row], pa, pb);
+            bnd[(c * 2 + 0) * 2 * d + j] = pa;
+            bnd[(c * 2 + 1) * 2 * d + j] = pb;
+        }
+        V *R = E::run(X, Y, TK, fd, +1);
+        V *prw = (V *)a.pr;
+        const T inz = (T)1 / (T)nz, Lz = (T)g.Lz;
+        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            if (c >= nv) continue;
+            V pa, pb;
+            lap_profile_t<T>(lcol[c], g.ZZ<T>(k), Lz, pa, pb);
+            const V dv = R[E::pos(k, fd) * TK + c];
+            prw[colq(k, c)] = mk<T>(dv.x * inz + pa.x, dv.y * inz + pa.y);
         }
         __syncthreads();
-        fc_continuation_fn<T>(g, X, TK, [&](int c, int j) { return bnd[c * 2 * d + j]; },
-                              [&](int c, int j) { return bnd[c * 2 * d + d + j]; });
+    }
+    // ---- 5. harmonic correction: a and b profiles (bulk rows in the kernel's precision, the
+    //         continuation from the FP64 rows), forward transformed
+    for (int which = 0; which < 2; which++) {
+        const T Lz = (T)g.Lz;
+        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            V pa, pb;
+            lap_profile_t<T>(lcol[c], g.ZZ<T>(k), Lz, pa, pb);
+            X[idx] = which == 0 ? pa : pb;
+        }
+        __syncthreads();
+        fc_continuation_fn<T>(g, X, TK, [&](int c, int j) { return bnd[(c * 2 + which) * 2 * d + j]; },
+                              [&](int c, int j) { return bnd[(c * 2 + which) * 2 * d + d + j]; });
         __syncthreads();
         V *R = E::run(X, Y, TK, fd, -1);
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
@@ -259,8 +328,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
             const V p = R[E::pos(k, fd) * TK + c];
             if (which == 0) {
                 const int kx = min(kx0 + c, g.nxh - 1);
-                U[idx] = csub(U[idx], cimk((T)g.kx[kx], p));
-                U[(size_t)nz * TK + idx] = csub(U[(size_t)nz * TK + idx], cimk((T)g.ky[ky], p));
+                U[idx] = csub(U[idx], cimk(g.KX<T>(kx), p));
+                U[(size_t)nz * TK + idx] = csub(U[(size_t)nz * TK + idx], cimk(g.KY<T>(ky), p));
             } else {
                 U[(size_t)2 * nz * TK + idx] = csub(U[(size_t)2 * nz * TK + idx], p);
             }
@@ -292,31 +361,48 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
     const int nv = min(TK, g.nxh - kx0);
     auto colq = [&](int z, int c) { return fidx<T>(g, z, ky, kx0 + c); };
     const T dt = (T)a.dt, kap = (T)a.kappa, rmp = (T)a.rmp, inz = (T)1 / (T)nz;
-    // 1. NL_theta forward, heat current, filter, laplak, update
+    // 1. NL_theta forward, heat current, filter, laplak, update.  vz is copied into Th while
+    //    NL_theta is transformed; theta and cold go into the FFT buffer afterwards.
     {
-        const V *nl = (const V *)a.nl[3];
-        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
-            X[idx] = c < nv ? nl[colq(k, c)] : mk<T>(0, 0);
-        }
+        const size_t tile = (size_t)nz * TK;
+        const size_t zs = (size_t)g.ny * g.ldx, col0 = (size_t)ky * g.ldx + kx0;
+        const bool stage2 = (size_t)E::kBuffers * L >= 2 * (size_t)nz;
+        tile_load_async(X, (const V *)a.nl[3] + col0, zs, nzp, TK, nv);
+        tile_load_async(Th, (const V *)a.vin[2] + col0, zs, nz, TK, nv);
+        async_wait_n<1>();
         __syncthreads();
         fc_continuation<T>(g, X, TK);
         __syncthreads();
         V *R = E::run(X, Y, TK, fd, -1);
-        const V *vz = (const V *)a.vin[2], *th = (const V *)a.vin[3], *cold = (const V *)a.cold[3];
+        async_wait();
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+            const int k = idx / TK, c = idx % TK;
+            V n = mk<T>(0, 0);
+            if (c < nv) {
+                const int kx = kx0 + c;
+                n = R[E::pos(k, fd) * TK + c];
+                const V w = Th[idx];
+                n = mk<T>(n.x - (T)a.xtemp * w.x, n.y - (T)a.xtemp * w.y);
+                n = cscale(n, g.FX<T>(kx));
+                n = cscale(n, g.FY<T>(ky));
+                n = cscale(n, g.FZ<T>(k));
+            }
+            Th[idx] = n;
+        }
+        __syncthreads();
+        const V *cold = (const V *)a.cold[3];
+        tile_load_async(X, (const V *)a.vin[3] + col0, zs, nz, TK, nv);
+        if (stage2) tile_load_async(X + tile, cold + col0, zs, nz, TK, nv);
+        async_wait();
+        __syncthreads();
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
             const int k = idx / TK, c = idx % TK;
             if (c >= nv) { Th[idx] = mk<T>(0, 0); continue; }
             const int kx = kx0 + c;
-            const size_t q = colq(k, c);
-            V n = R[E::pos(k, fd) * TK + c];
-            const V w = vz[q];
-            n = mk<T>(n.x - (T)a.xtemp * w.x, n.y - (T)a.xtemp * w.y);
-            n = cscale(n, (T)g.fx[kx]);
-            n = cscale(n, (T)g.fy[ky]);
-            n = cscale(n, (T)g.fz[k]);
-            const T k2 = (T)g.kx[kx] * (T)g.kx[kx] + (T)g.ky[ky] * (T)g.ky[ky] + (T)g.kz[k] * (T)g.kz[k];
-            const V t = th[q], cv = cold[q];
+            const T k2 = g.KX<T>(kx) * g.KX<T>(kx) + g.KY<T>(ky) * g.KY<T>(ky) + g.KZ<T>(k) * g.KZ<T>(k);
+            const V t = X[idx], cv = stage2 ? X[tile + idx] : cold[colq(k, c)];
+            const V n = Th[idx];
             const V lap = cscale(t, -k2);
             Th[idx] = mk<T>(cv.x + dt * (kap * lap.x - n.x) * rmp, cv.y + dt * (kap * lap.y - n.y) * rmp);
         }
@@ -341,9 +427,9 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
             const int k = idx / TK, c = idx % TK;
             const int kx = min(kx0 + c, g.nxh - 1);
             V v = R[E::pos(k, fd) * TK + c];
-            v = cscale(v, (T)g.fx[kx]);
-            v = cscale(v, (T)g.fy[ky]);
-            v = cscale(v, (T)g.fz[k]);
+            v = cscale(v, g.FX<T>(kx));
+            v = cscale(v, g.FY<T>(ky));
+            v = cscale(v, g.FZ<T>(k));
             Th[idx] = v;
         }
         __syncthreads();

@@ -16,7 +16,8 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
     const int d = P.oz;
     auto smem = [&](int tk) -> size_t {
         if (which == kFusedVelocity)
-            return (3 * (size_t)P.nz + E::kBuffers * L) * tk * es + (2 * (size_t)kThreads + (size_t)tk * (2 + 2 * d)) * 16;
+            return (3 * (size_t)P.nz + E::kBuffers * L) * tk * es + (2 * (size_t)kThreads + (size_t)tk * (2 + 4 * d)) * 16 +
+                   (size_t)tk * sizeof(LapCol<T>);
         if (which == kFusedTheta) return ((size_t)P.nz + E::kBuffers * L) * tk * es;
         return E::kBuffers * L * 2 * es;
     };

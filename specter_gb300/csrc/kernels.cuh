@@ -69,6 +69,7 @@ struct ZInvArgs {
     int nrows;
     int scale_rows;   // rows [0, scale_rows) scaled, the rest copied unscaled
     double scale;
+    int staged;       // 1: the input tile is staged once in smem (some field has two outputs)
 };
 
 template <typename T, class E>
@@ -76,18 +77,30 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_inverse(Geo g, ty
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * TK;
+    V *S = X + (size_t)E::kBuffers * fd.L * TK;  // staged input tile (a.staged)
     const int kx0 = blockIdx.x * TK, ky = blockIdx.y, f = blockIdx.z;
     const V *in = (const V *)a.in[f];
     const int nv = min(TK, g.nxh - kx0);
+    const size_t zstride = (size_t)g.ny * g.ldx;
+    const V *src = in + (size_t)ky * g.ldx + kx0;
+    if (a.staged) tile_load_async(S, src, zstride, g.nz, TK, nv);
     for (int pass = 1; pass >= 0; pass--) {  // derivative output first: out0 may alias in
         V *out = (V *)(pass == 0 ? a.out0[f] : a.out1[f]);
         if (!out) continue;
-        for (int idx = threadIdx.x; idx < g.nz * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
-            V v = mk<T>(0, 0);
-            if (c < nv) v = in[fidx<T>(g, k, ky, kx0 + c)];
-            if (pass == 1) v = cimk((T)g.kz[k], v);
-            X[idx] = v;
+        if (a.staged) {
+            async_wait();
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < g.nz * TK; idx += blockDim.x) {
+                const V v = S[idx];
+                X[idx] = pass == 1 ? cimk(g.KZ<T>(idx / TK), v) : v;
+            }
+        } else {
+            tile_load_async(X, src, zstride, g.nz, TK, nv);
+            async_wait();
+            if (pass == 1) {
+                __syncthreads();
+                for (int idx = threadIdx.x; idx < g.nz * TK; idx += blockDim.x) X[idx] = cimk(g.KZ<T>(idx / TK), X[idx]);
+            }
         }
         __syncthreads();
         V *R = E::run(X, Y, TK, fd, +1);
@@ -146,11 +159,11 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_forward(Geo g, ty
     V *out = (V *)a.out[f];
     const int nv = min(TK, g.nxh - kx0);
     const T s = (T)a.in_scale;
-    for (int idx = threadIdx.x; idx < g.nzp * TK; idx += blockDim.x) {
-        const int k = idx / TK, c = idx % TK;
-        V v = mk<T>(0, 0);
-        if (c < nv) v = in[fidx<T>(g, k, ky, kx0 + c)];
-        X[idx] = a.in_scale != 1.0 ? cscale(v, s) : v;
+    tile_load_async(X, in + (size_t)ky * g.ldx + kx0, (size_t)g.ny * g.ldx, g.nzp, TK, nv);
+    async_wait();
+    if (a.in_scale != 1.0) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < g.nzp * TK; idx += blockDim.x) X[idx] = cscale(X[idx], s);
     }
     __syncthreads();
     fc_continuation<T>(g, X, TK);
@@ -171,6 +184,7 @@ struct YArgs {
     void *out1[kMaxF];
     int sign;
     double scale;
+    int staged;       // 1: the input tile is staged once in smem (some field has two outputs)
 };
 
 template <typename T, class E>
@@ -178,18 +192,29 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass(Geo g, typen
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * TK;
+    V *S = X + (size_t)E::kBuffers * fd.L * TK;  // staged input tile (a.staged)
     const int kx0 = blockIdx.x * TK, z = blockIdx.y, f = blockIdx.z;
     const V *in = (const V *)a.in[f];
     const int nv = min(TK, g.nxh - kx0);
+    const V *src = in + (size_t)z * g.ny * g.ldx + kx0;
+    if (a.staged) tile_load_async(S, src, (size_t)g.ldx, g.ny, TK, nv);
     for (int pass = 1; pass >= 0; pass--) {  // derivative output first: out0 may alias in
         V *out = (V *)(pass == 0 ? a.out0[f] : a.out1[f]);
         if (!out) continue;
-        for (int idx = threadIdx.x; idx < g.ny * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
-            V v = mk<T>(0, 0);
-            if (c < nv) v = in[fidx<T>(g, z, k, kx0 + c)];
-            if (pass == 1) v = cimk((T)g.ky[k], v);
-            X[idx] = v;
+        if (a.staged) {
+            async_wait();
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < g.ny * TK; idx += blockDim.x) {
+                const V v = S[idx];
+                X[idx] = pass == 1 ? cimk(g.KY<T>(idx / TK), v) : v;
+            }
+        } else {
+            tile_load_async(X, src, (size_t)g.ldx, g.ny, TK, nv);
+            async_wait();
+            if (pass == 1) {
+                __syncthreads();
+                for (int idx = threadIdx.x; idx < g.ny * TK; idx += blockDim.x) X[idx] = cimk(g.KY<T>(idx / TK), X[idx]);
+            }
         }
         __syncthreads();
         V *R = E::run(X, Y, TK, fd, a.sign);
@@ -263,15 +288,9 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_r2c(Geo g, typena
     const T *in = (const T *)a.in[f];
     V *out = (V *)a.out[f];
     const int H = g.H;
-    for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
-        const int m = idx / RB, r = idx % RB;
-        V v = mk<T>(0, 0);
-        if (row0 + r < nrows) {
-            const T *p = in + (size_t)(row0 + r) * g.nx + 2 * m;
-            v = mk<T>(p[0], p[1]);
-        }
-        X[idx] = v;
-    }
+    // packed real row: element m = (x_{2m}, x_{2m+1})
+    rows_load_async(X, (const V *)(in + (size_t)row0 * g.nx), (size_t)H, H, RB, min(RB, nrows - row0));
+    async_wait();
     __syncthreads();
     V *R = E::run(X, Y, RB, fd, -1);
     r2c_post<T, E>(g, fd, R, S, RB);
@@ -296,12 +315,8 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_c2r(Geo g, typena
     const int row0 = blockIdx.x * RB, nrows = a.nrows * g.ny;
     const V *in = (const V *)a.in[f];
     T *out = (T *)a.out[f];
-    for (int idx = threadIdx.x; idx < g.nxh * RB; idx += blockDim.x) {
-        const int r = idx / g.nxh, k = idx % g.nxh;
-        V v = mk<T>(0, 0);
-        if (row0 + r < nrows) v = in[(size_t)(row0 + r) * g.ldx + k];
-        S[k * RB + r] = v;
-    }
+    rows_load_async(S, in + (size_t)row0 * g.ldx, (size_t)g.ldx, g.nxh, RB, min(RB, nrows - row0));
+    async_wait();
     __syncthreads();
     c2r_pre<T>(g, S, X, RB);
     __syncthreads();
@@ -338,89 +353,93 @@ struct XNLArgs {
     double tmp;          // 1/(nx ny nz)^2
 };
 
+// Input t of the x pass: t < 3 velocity rows, then per component u (times i kx), d/dy, d/dz.
 template <typename T>
-__device__ __forceinline__ void load_row_spec(const Geo &g, const C2<T> *in, C2<T> *S, int row0, int nrows, int RB, int dx) {
-    using V = C2<T>;
-    for (int idx = threadIdx.x; idx < g.nxh * RB; idx += blockDim.x) {
-        const int r = idx / g.nxh, k = idx % g.nxh;
-        V v = mk<T>(0, 0);
-        if (row0 + r < nrows) v = in[(size_t)(row0 + r) * g.ldx + k];
-        if (dx) v = cimk((T)g.kx[k], v);
-        S[k * RB + r] = v;
-    }
-}
-
-// C2R of a spectral row set held in S into P (H x RB packed physical, natural order)
-template <typename T, class E>
-__device__ __forceinline__ void c2r_rows(const Geo &g, const typename E::Desc &fd, C2<T> *S, C2<T> *X, C2<T> *Y,
-                                         C2<T> *P, int RB) {
-    __syncthreads();
-    c2r_pre<T>(g, S, X, RB);
-    __syncthreads();
-    C2<T> *R = E::run(X, Y, RB, fd, +1);
-    for (int idx = threadIdx.x; idx < g.H * RB; idx += blockDim.x) {
-        const int m = idx / RB, r = idx % RB;
-        P[idx] = R[E::pos(m, fd) * RB + r];
-    }
-    __syncthreads();
+__device__ __forceinline__ const C2<T> *xnl_input(const XNLArgs &a, int t, int &dx) {
+    const int nc = a.c1 - a.c0;
+    dx = 0;
+    if (t < 3) return (const C2<T> *)a.u[t];
+    t -= 3;
+    const int term = t / nc, i = a.c0 + t % nc;
+    if (term == 0) { dx = 1; return (const C2<T> *)a.u[i]; }
+    return (const C2<T> *)(term == 1 ? a.dy[i] : a.dz[i]);
 }
 
 template <typename T, class E>
 __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, typename E::Desc fd, XNLArgs a, int RB) {
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int H = g.H, L = fd.L;
+    const int H = g.H, L = fd.L, nxh = g.nxh;
     V *X = (V *)smem_raw;
     V *Y = X + (size_t)L * RB;
-    V *S = X + (size_t)E::kBuffers * L * RB;   // nxh * RB spectral row staging
-    V *U = S + (size_t)g.nxh * RB;              // 3 * H * RB physical velocity rows
+    V *Sb[2];
+    Sb[0] = X + (size_t)E::kBuffers * L * RB;   // two nxh * RB spectral row stagings (prefetch)
+    Sb[1] = Sb[0] + (size_t)nxh * RB;
+    V *U = Sb[1] + (size_t)nxh * RB;            // 3 * H * RB physical velocity rows
     V *P = U + (size_t)3 * H * RB;              // H * RB product operand
     V *A = P + (size_t)H * RB;                  // (c1-c0) * H * RB accumulators
-    const int c0 = a.c0, c1 = a.c1;
+    const int c0 = a.c0, c1 = a.c1, nc = c1 - c0;
     const int row0 = blockIdx.x * RB, nrows = a.nrows * g.ny;
-    for (int j = 0; j < 3; j++) {
-        load_row_spec<T>(g, (const V *)a.u[j], S, row0, nrows, RB, 0);
-        c2r_rows<T, E>(g, fd, S, X, Y, U + (size_t)j * H * RB, RB);
-    }
-    // term 1: u_x * d/dx v_i (and theta)
-    for (int i = c0; i < c1; i++) {
-        load_row_spec<T>(g, (const V *)a.u[i], S, row0, nrows, RB, 1);
-        c2r_rows<T, E>(g, fd, S, X, Y, P, RB);
-        for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
-            const V u = U[idx], p = P[idx];
-            A[(size_t)(i - c0) * H * RB + idx] = mk<T>(u.x * p.x, u.y * p.y);
-        }
-    }
-    // term 2: + u_y * d/dy v_i
-    for (int i = c0; i < c1; i++) {
-        load_row_spec<T>(g, (const V *)a.dy[i], S, row0, nrows, RB, 0);
-        c2r_rows<T, E>(g, fd, S, X, Y, P, RB);
-        for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
-            const V u = U[(size_t)H * RB + idx], p = P[idx];
-            V &acc = A[(size_t)(i - c0) * H * RB + idx];
-            acc = mk<T>(acc.x + u.x * p.x, acc.y + u.y * p.y);
-        }
-    }
-    // term 3: (acc + u_z * d/dz v_i) * tmp, then R2C
+    const int nv = min(RB, nrows - row0);
+    const int T_in = 3 + 3 * nc;
     const T tmp = (T)a.tmp;
-    for (int i = c0; i < c1; i++) {
-        load_row_spec<T>(g, (const V *)a.dz[i], S, row0, nrows, RB, 0);
-        c2r_rows<T, E>(g, fd, S, X, Y, P, RB);
-        for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
-            const V u = U[(size_t)2 * H * RB + idx], p = P[idx];
-            const V acc = A[(size_t)(i - c0) * H * RB + idx];
-            X[idx] = mk<T>((acc.x + u.x * p.x) * tmp, (acc.y + u.y * p.y) * tmp);
+    int dx;
+    rows_load_async(Sb[0], xnl_input<T>(a, 0, dx) + (size_t)row0 * g.ldx, (size_t)g.ldx, nxh, RB, nv);
+    for (int t = 0; t < T_in; t++) {
+        V *S = Sb[t & 1];
+        async_wait();
+        __syncthreads();  // input t is in S; every thread is done with the previous iteration
+        if (t + 1 < T_in) {
+            int dx1;
+            const V *nxt = xnl_input<T>(a, t + 1, dx1);
+            rows_load_async(Sb[(t + 1) & 1], nxt + (size_t)row0 * g.ldx, (size_t)g.ldx, nxh, RB, nv);
         }
-        __syncthreads();
-        V *R = E::run(X, Y, RB, fd, -1);
-        r2c_post<T, E>(g, fd, R, S, RB);
-        __syncthreads();
-        V *out = (V *)a.out[i];
-        for (int idx = threadIdx.x; idx < g.nxh * RB; idx += blockDim.x) {
-            const int r = idx / g.nxh, k = idx % g.nxh;
-            if (row0 + r < nrows) out[(size_t)(row0 + r) * g.ldx + k] = S[k * RB + r];
+        xnl_input<T>(a, t, dx);
+        if (dx) {
+            for (int idx = threadIdx.x; idx < nxh * RB; idx += blockDim.x) S[idx] = cimk(g.KX<T>(idx / RB), S[idx]);
+            __syncthreads();
         }
+        c2r_pre<T>(g, S, X, RB);
         __syncthreads();
+        V *R = E::run(X, Y, RB, fd, +1);
+        const int term = t < 3 ? -1 : (t - 3) / nc, i = t < 3 ? t : c0 + (t - 3) % nc;
+        if (term < 2) {
+            for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
+                const int m = idx / RB, r = idx % RB;
+                const V p = R[E::pos(m, fd) * RB + r];
+                if (term < 0) {
+                    U[(size_t)i * H * RB + idx] = p;
+                } else if (term == 0) {
+                    const V u = U[idx];
+                    A[(size_t)(i - c0) * H * RB + idx] = mk<T>(u.x * p.x, u.y * p.y);
+                } else {
+                    const V u = U[(size_t)H * RB + idx];
+                    V &acc = A[(size_t)(i - c0) * H * RB + idx];
+                    acc = mk<T>(acc.x + u.x * p.x, acc.y + u.y * p.y);
+                }
+            }
+        } else {
+            // term 3: (acc + u_z d/dz v_i) * tmp, forward R2C, store
+            for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
+                const int m = idx / RB, r = idx % RB;
+                P[idx] = R[E::pos(m, fd) * RB + r];
+            }
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
+                const V u = U[(size_t)2 * H * RB + idx], p = P[idx];
+                const V acc = A[(size_t)(i - c0) * H * RB + idx];
+                X[idx] = mk<T>((acc.x + u.x * p.x) * tmp, (acc.y + u.y * p.y) * tmp);
+            }
+            __syncthreads();
+            R = E::run(X, Y, RB, fd, -1);
+            r2c_post<T, E>(g, fd, R, S, RB);  // S (input t) is consumed: reuse it for the output
+            __syncthreads();
+            V *out = (V *)a.out[i];
+            for (int idx = threadIdx.x; idx < nxh * RB; idx += blockDim.x) {
+                const int r = idx / nxh, k = idx % nxh;
+                if (r < nv) out[(size_t)(row0 + r) * g.ldx + k] = S[k * RB + r];
+            }
+        }
     }
 }
 

@@ -23,7 +23,7 @@ namespace sg {
 
 template <typename T>
 __device__ __forceinline__ T kk2_at(const Geo &g, int z, int ky, int kx) {
-    const T a = (T)g.kx[kx], b = (T)g.ky[ky], c = (T)g.kz[z];
+    const T a = g.KX<T>(kx), b = g.KY<T>(ky), c = g.KZ<T>(z);
     return a * a + b * b + c * c;
 }
 
@@ -31,7 +31,7 @@ __device__ __forceinline__ T kk2_at(const Geo &g, int z, int ky, int kx) {
 template <typename T>
 __global__ void k_derivk(Geo g, const C2<T> *a, C2<T> *b, int dir) {
     SG_ELEMS_BEGIN(g, 0, g.nz)
-        const T k = (T)(dir == 1 ? g.kx[kx] : dir == 2 ? g.ky[ky] : g.kz[z]);
+        const T k = dir == 1 ? g.KX<T>(kx) : dir == 2 ? g.KY<T>(ky) : g.KZ<T>(z);
         b[q] = cimk(k, a[q]);
     SG_ELEMS_END
 }
@@ -46,7 +46,7 @@ __global__ void k_laplak(Geo g, const C2<T> *a, C2<T> *b) {
 template <typename T>
 __global__ void k_curlk(Geo g, const C2<T> *a, const C2<T> *b, C2<T> *c, int dir) {
     SG_ELEMS_BEGIN(g, 0, g.nz)
-        const T kx_ = (T)g.kx[kx], ky_ = (T)g.ky[ky], kz_ = (T)g.kz[z];
+        const T kx_ = g.KX<T>(kx), ky_ = g.KY<T>(ky), kz_ = g.KZ<T>(z);
         C2<T> r;
         if (dir == 1) r = csub(cimk(ky_, b[q]), cimk(kz_, a[q]));
         else if (dir == 2) r = csub(cimk(kz_, a[q]), cimk(kx_, b[q]));
@@ -60,9 +60,9 @@ template <typename T>
 __global__ void k_filter(Geo g, C2<T> *a) {
     SG_ELEMS_BEGIN(g, 0, g.nz)
         C2<T> v = a[q];
-        v = cscale(v, (T)g.fx[kx]);
-        v = cscale(v, (T)g.fy[ky]);
-        v = cscale(v, (T)g.fz[z]);
+        v = cscale(v, g.FX<T>(kx));
+        v = cscale(v, g.FY<T>(ky));
+        v = cscale(v, g.FZ<T>(z));
         a[q] = v;
     SG_ELEMS_END
 }
@@ -92,9 +92,9 @@ __global__ void k_sub_scaled(Geo g, C2<T> *y, const C2<T> *x, double s) {
 template <typename T>
 __global__ void k_div(Geo g, const C2<T> *a, const C2<T> *b, const C2<T> *c, C2<T> *d) {
     SG_ELEMS_BEGIN(g, 0, g.nz)
-        C2<T> s = cimk((T)g.kx[kx], a[q]);
-        s = cadd(s, cimk((T)g.ky[ky], b[q]));
-        s = cadd(s, cimk((T)g.kz[z], c[q]));
+        C2<T> s = cimk(g.KX<T>(kx), a[q]);
+        s = cadd(s, cimk(g.KY<T>(ky), b[q]));
+        s = cadd(s, cimk(g.KZ<T>(z), c[q]));
         d[q] = s;
     SG_ELEMS_END
 }
@@ -110,7 +110,7 @@ __global__ void k_kk2_mul(Geo g, const C2<T> *a, C2<T> *b) {
 template <typename T>
 __global__ void k_poisson(Geo g, C2<T> *a, C2<T> *b, C2<T> *c, C2<T> *d, C2<T> *C1, int bctarget) {
     SG_ELEMS_BEGIN(g, 0, g.nz)
-        const T kx_ = (T)g.kx[kx], ky_ = (T)g.ky[ky], kz_ = (T)g.kz[z];
+        const T kx_ = g.KX<T>(kx), ky_ = g.KY<T>(ky), kz_ = g.KZ<T>(z);
         const T k2 = kk2_at<T>(g, z, ky, kx);
         C2<T> A = a[q], B = b[q], Cc = c[q];
         C2<T> s = mk<T>(kx_ * A.x + ky_ * B.x + kz_ * Cc.x, kx_ * A.y + ky_ * B.y + kz_ * Cc.y);
@@ -130,8 +130,8 @@ template <typename T>
 __global__ void k_proj_sub(Geo g, C2<T> *a, C2<T> *b, C2<T> *c, const C2<T> *A2, const C2<T> *A3) {
     SG_ELEMS_BEGIN(g, 0, g.nz)
         const C2<T> p = A2[q];
-        a[q] = csub(a[q], cimk((T)g.kx[kx], p));
-        b[q] = csub(b[q], cimk((T)g.ky[ky], p));
+        a[q] = csub(a[q], cimk(g.KX<T>(kx), p));
+        b[q] = csub(b[q], cimk(g.KY<T>(ky), p));
         c[q] = csub(c[q], A3[q]);
     SG_ELEMS_END
 }
@@ -218,8 +218,8 @@ __global__ void k_noslip(Geo g, C2<T> *vx, C2<T> *vy, const C2<T> *pr, double tm
         const int ind = w == 0 ? 0 : g.nzp - 1;
         const size_t q = fidx<T>(g, ind, ky, kx);
         const C2<T> p = pr[q];
-        vx[q] = cscale(cimk((T)g.kx[kx], p), (T)tmp);
-        vy[q] = cscale(cimk((T)g.ky[ky], p), (T)tmp);
+        vx[q] = cscale(cimk(g.KX<T>(kx), p), (T)tmp);
+        vy[q] = cscale(cimk(g.KY<T>(ky), p), (T)tmp);
         if (kx == 0 && ky == 0) {
             const double nn = (double)g.nx * g.ny;
             vx[q] = mk<T>((T)(nn * (w == 0 ? vb.x : vb.z)), (T)0);

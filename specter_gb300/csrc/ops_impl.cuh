@@ -65,12 +65,22 @@ static double cplx_rows(const Plan &P, double rows) { return rows * P.ny * P.nxh
 // Tile widths (kx columns per block for the y/z passes, rows per block for the x pass) are
 // runtime values: the largest power of two whose ping-pong buffers fit the smem budget.
 
+// 1 when some field of a two-output pass writes both outputs: its input tile is then read
+// from HBM once into a staging buffer instead of once per output.
+static int two_outputs(void *const out0[], void *const out1[], int nf) {
+    for (int f = 0; f < nf; f++)
+        if (out0[f] && out1[f]) return 1;
+    return 0;
+}
+
 template <typename T>
-static int launch_z_inverse(Plan &P, const ZInvArgs &a, int nf) {
+static int launch_z_inverse(Plan &P, const ZInvArgs &a0, int nf) {
     const size_t es = sizeof(C2<T>);
-    const int tk = pick_tile(2 * (size_t)P.tz.d.L * es);
+    ZInvArgs a = a0;
+    a.staged = two_outputs(a.out0, a.out1, nf);
+    const int tk = pick_tile((2 * (size_t)P.tz.d.L + (a.staged ? P.nz : 0)) * es);
     if (!tk) { set_error("z length too large for shared memory"); return ERR_SHAPE; }
-    const size_t sm = 2 * (size_t)P.tz.d.L * tk * es;
+    const size_t sm = (2 * (size_t)P.tz.d.L + (a.staged ? P.nz : 0)) * tk * es;
     double bytes = 0;
     for (int f = 0; f < nf; f++)
         bytes += cplx_rows(P, P.nz) + cplx_rows(P, a.nrows) * ((a.out0[f] ? 1 : 0) + (a.out1[f] ? 1 : 0) + (a.add[f] ? 1 : 0));
@@ -98,11 +108,13 @@ static int launch_z_forward(Plan &P, const ZFwdArgs &a, int nf) {
 }
 
 template <typename T>
-static int launch_y(Plan &P, const YArgs &a, int nf, int nplanes) {
+static int launch_y(Plan &P, const YArgs &a0, int nf, int nplanes) {
     const size_t es = sizeof(C2<T>);
-    const int tk = pick_tile(2 * (size_t)P.ty.d.L * es);
+    YArgs a = a0;
+    a.staged = two_outputs(a.out0, a.out1, nf);
+    const int tk = pick_tile((2 * (size_t)P.ty.d.L + (a.staged ? P.ny : 0)) * es);
     if (!tk) { set_error("y length too large for shared memory"); return ERR_SHAPE; }
-    const size_t sm = 2 * (size_t)P.ty.d.L * tk * es;
+    const size_t sm = (2 * (size_t)P.ty.d.L + (a.staged ? P.ny : 0)) * tk * es;
     double bytes = 0;
     for (int f = 0; f < nf; f++) bytes += cplx_rows(P, nplanes) * (1 + (a.out0[f] ? 1 : 0) + (a.out1[f] ? 1 : 0));
     const int fst = fast_y(P, a, nf, nplanes, bytes);
@@ -140,7 +152,7 @@ static int launch_x(Plan &P, const XArgs &a, int nf, bool r2c) {
 template <typename T>
 static int launch_x_nl(Plan &P, const XNLArgs &a) {
     const size_t es = sizeof(C2<T>);
-    const size_t per = (2 * (size_t)P.tx.d.L + P.nxh + (4 + (a.c1 - a.c0)) * (size_t)P.H) * es;
+    const size_t per = (2 * (size_t)P.tx.d.L + 2 * (size_t)P.nxh + (4 + (a.c1 - a.c0)) * (size_t)P.H) * es;
     const int rb = pick_tile(per);
     if (!rb) { set_error("x length too large for shared memory"); return ERR_SHAPE; }
     const size_t sm = per * rb;

@@ -196,6 +196,11 @@ int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], cons
     size_t ofx = app(p->fx), ofy = app(p->fy), ofz = app(p->fz);
     if (cudaMalloc(&p->dgeo, g.size() * sizeof(double)) != cudaSuccess) { set_error("cudaMalloc failed"); delete p; return ERR_OOM; }
     cudaMemcpy(p->dgeo, g.data(), g.size() * sizeof(double), cudaMemcpyHostToDevice);
+    {
+        std::vector<float> gf(g.begin(), g.end());
+        if (cudaMalloc(&p->dgeof, gf.size() * sizeof(float)) != cudaSuccess) { set_error("cudaMalloc failed"); plan_destroy(p); return ERR_OOM; }
+        cudaMemcpy(p->dgeof, gf.data(), gf.size() * sizeof(float), cudaMemcpyHostToDevice);
+    }
     // R2C / C2R post-processing twiddles exp(-2*pi*i*k/nx), k = 0..H
     {
         const size_t es = p->elt();
@@ -224,6 +229,8 @@ int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], cons
     G.ldx = p->ldx; G.H = p->H; G.Lz = p->Lz;
     G.kx = p->dgeo + okx; G.ky = p->dgeo + oky; G.kz = p->dgeo + okz; G.z = p->dgeo + oz_;
     G.dir = p->dgeo + odir; G.fx = p->dgeo + ofx; G.fy = p->dgeo + ofy; G.fz = p->dgeo + ofz;
+    G.kxf = p->dgeof + okx; G.kyf = p->dgeof + oky; G.kzf = p->dgeof + okz; G.zf = p->dgeof + oz_;
+    G.fxf = p->dgeof + ofx; G.fyf = p->dgeof + ofy; G.fzf = p->dgeof + ofz;
     G.xtw = p->dxtw;
     p->nred = 4096;
     cudaMalloc(&p->dred, sizeof(double) * p->nred);
@@ -306,6 +313,7 @@ void plan_destroy(Plan *p) {
     free_fft_table(p->tx); free_fft_table(p->ty); free_fft_table(p->tz);
     free_fft4_table(p->tx4); free_fft4_table(p->ty4); free_fft4_table(p->tz4);
     if (p->dgeo) cudaFree(p->dgeo);
+    if (p->dgeof) cudaFree(p->dgeof);
     if (p->dxtw) cudaFree(p->dxtw);
     if (p->dred) cudaFree(p->dred);
     if (p->dwtw) cudaFree(p->dwtw);

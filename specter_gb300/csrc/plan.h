@@ -42,9 +42,23 @@ struct Geo {
     int nx, ny, nz, cz, oz, nxh, nzp, ldx, H;
     const double *kx, *ky, *kz, *z, *dir;     // device, FP64
     const double *fx, *fy, *fz;               // fc_filter factors per axis (FP64)
+    const float *kxf, *kyf, *kzf, *zf;         // the same tables rounded to FP32, so FP32
+    const float *fxf, *fyf, *fzf;             // kernels do no FP64 conversion per element
     const void *xtw;                          // C2<T>[H+1]: exp(-2*pi*i*k/nx)
     const void *wtw;                          // double2[nz]: exp(+2*pi*i*k*(nzp-1)/nz)
     double Lz;
+    // table entries in the kernel's precision: (T)kx[i], read from the matching table
+#define SG_GEO_TABLE(NAME, D, F) \
+    template <typename T> __device__ __forceinline__ T NAME(int i) const { \
+        if constexpr (sizeof(T) == 8) return __ldg(D + i); else return __ldg(F + i); }
+    SG_GEO_TABLE(KX, kx, kxf)
+    SG_GEO_TABLE(KY, ky, kyf)
+    SG_GEO_TABLE(KZ, kz, kzf)
+    SG_GEO_TABLE(ZZ, z, zf)
+    SG_GEO_TABLE(FX, fx, fxf)
+    SG_GEO_TABLE(FY, fy, fyf)
+    SG_GEO_TABLE(FZ, fz, fzf)
+#undef SG_GEO_TABLE
 };
 
 struct Plan {
@@ -53,6 +67,7 @@ struct Plan {
     double Lx = 1, Ly = 1, Lz = 1, Dkx = 1, Dky = 1, Dkz = 1, dz = 1;
     std::vector<double> kx, ky, kz, z, dir, fx, fy, fz;
     double *dgeo = nullptr;   // device block holding kx, ky, kz, z, dir, fx, fy, fz
+    float *dgeof = nullptr;   // the same block rounded to FP32
     void *dxtw = nullptr;
     FFTTable tx, ty, tz;      // lengths H = nx/2, ny, nz
     FFT4Table tx4, ty4, tz4;  // four-step tables of the same lengths (FP32 plans)
