@@ -63,14 +63,16 @@ __device__ __forceinline__ void tile_load_async(V *dst, const V *src, size_t str
     async_commit();
 }
 
-// Same for rows stored contiguously: element (k, c) of the [rows][TK] tile comes from
-// src[c*cstride + k] (c < nv), so consecutive threads read consecutive k.
+// Same for rows stored contiguously: element (k, c) of the [rows][TK] tile, held at
+// dst[k*dstride + c], comes from src[c*cstride + k] (c < nv), so consecutive threads read
+// consecutive k.  An odd dstride (TK + 1) keeps those shared-memory writes free of bank conflicts.
 template <typename V>
-__device__ __forceinline__ void rows_load_async(V *dst, const V *src, size_t cstride, int rows, int TK, int nv) {
+__device__ __forceinline__ void rows_load_async(V *dst, const V *src, size_t cstride, int rows, int TK, int nv,
+                                                int dstride) {
     for (int idx = threadIdx.x; idx < rows * TK; idx += blockDim.x) {
         const int c = idx / rows, k = idx % rows;
-        if (c < nv) cp_async<sizeof(V)>(dst + k * TK + c, src + (size_t)c * cstride + k);
-        else { V z; z.x = 0; z.y = 0; dst[k * TK + c] = z; }
+        if (c < nv) cp_async<sizeof(V)>(dst + k * dstride + c, src + (size_t)c * cstride + k);
+        else { V z; z.x = 0; z.y = 0; dst[k * dstride + c] = z; }
     }
     async_commit();
 }

@@ -108,11 +108,21 @@ void free_fft4_table(FFT4Table &t) {
 
 namespace {
 constexpr size_t kFastBudget = 110 * 1024;  // two resident blocks per SM
+constexpr size_t kMaxSmem = 227 * 1024;     // one block per SM (largest dynamic allocation)
 
 int pick(size_t per, size_t budget = kFastBudget) {
     for (int t : {16, 8, 4, 2, 1})
         if (per * t <= budget) return t;
     return 0;
+}
+
+// Stage the input tile once (two-output passes) only when that keeps the tile width; otherwise
+// the second output re-reads the tile, which is then still in L2.
+int stage_tile(void *const out0[], void *const out1[], int nf, int L, int n) {
+    int two = 0;
+    for (int f = 0; f < nf; f++) two |= (out0[f] && out1[f]) ? 1 : 0;
+    if (!two) return 0;
+    return pick((size_t)L * sizeof(float2)) == pick(((size_t)L + n) * sizeof(float2)) ? 1 : 0;
 }
 
 template <typename K>
@@ -136,8 +146,7 @@ template <int L1, int L2>
 int zinv(Plan &P, const ZInvArgs &a0, int nf, double bytes) {
     using E = FourStep<float, L1, L2>;
     ZInvArgs a = a0;
-    a.staged = 0;
-    for (int f = 0; f < nf; f++) a.staged |= (a.out0[f] && a.out1[f]) ? 1 : 0;
+    a.staged = stage_tile(a.out0, a.out1, nf, P.tz4.d.L, P.nz);
     const size_t per = ((size_t)P.tz4.d.L + (a.staged ? P.nz : 0)) * sizeof(float2);
     const int tk = pick(per);
     const size_t sm = per * tk;
@@ -162,8 +171,7 @@ template <int L1, int L2>
 int ypass(Plan &P, const YArgs &a0, int nf, int nplanes, double bytes) {
     using E = FourStep<float, L1, L2>;
     YArgs a = a0;
-    a.staged = 0;
-    for (int f = 0; f < nf; f++) a.staged |= (a.out0[f] && a.out1[f]) ? 1 : 0;
+    a.staged = stage_tile(a.out0, a.out1, nf, P.ty4.d.L, P.ny);
     const size_t per = ((size_t)P.ty4.d.L + (a.staged ? P.ny : 0)) * sizeof(float2);
     const int tk = pick(per);
     const size_t sm = per * tk;
@@ -176,9 +184,11 @@ int ypass(Plan &P, const YArgs &a0, int nf, int nplanes, double bytes) {
 template <int L1, int L2>
 int xpass(Plan &P, const XArgs &a, int nf, bool r2c, double bytes) {
     using E = FourStep<float, L1, L2>;
-    const size_t per = ((size_t)P.tx4.d.L + P.nxh) * sizeof(float2);
-    const int rb = pick(per);
-    const size_t sm = per * rb;
+    int rb = 0;
+    for (int t : {16, 8, 4, 2, 1})
+        if (x_pass_elems<E>(P.tx4.d, P.nxh, t) * sizeof(float2) <= kFastBudget) { rb = t; break; }
+    if (!rb) return kNoFast;
+    const size_t sm = x_pass_elems<E>(P.tx4.d, P.nxh, rb) * sizeof(float2);
     const dim3 grid(cdiv(a.nrows * P.ny, rb), 1, nf);
     if (r2c) {
         smem_attr(k_x_r2c<float, E>, sm);
@@ -195,10 +205,11 @@ int xpass(Plan &P, const XArgs &a, int nf, bool r2c, double bytes) {
 template <int L1, int L2>
 int xnl(Plan &P, const XNLArgs &a, double bytes) {
     using E = FourStep<float, L1, L2>;
-    const size_t per = ((size_t)P.tx4.d.L + 2 * (size_t)P.nxh + (4 + (a.c1 - a.c0)) * (size_t)P.H) * sizeof(float2);
-    const int rb = pick(per, 200 * 1024);
+    int rb = 0;
+    for (int t : {16, 8, 4, 2, 1})
+        if (x_nl_elems<E>(P.tx4.d, P.nxh, P.H, t) * sizeof(float2) <= kMaxSmem) { rb = t; break; }
     if (!rb) return kNoFast;
-    const size_t sm = per * rb;
+    const size_t sm = x_nl_elems<E>(P.tx4.d, P.nxh, P.H, rb) * sizeof(float2);
     smem_attr(k_x_nonlinear<float, E>, sm);
     Scope s(P, "x_nonlinear", bytes);
     k_x_nonlinear<float, E><<<dim3(cdiv(a.nrows * P.ny, rb)), kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a, rb);

@@ -192,22 +192,27 @@ __device__ __forceinline__ void fft4_pn(C2<T> *X, int B, const FFT4Desc &d) {
 template <int L1, int L2>
 __device__ __forceinline__ int perm_pos(int k) { return L2 * (k % L1) + k / L1; }
 
-// ---- Bluestein over L = L1*L2: natural rows [0, n) in, natural rows [0, n) out (SIGN) ------------
-// Rows [n, L) of X are zeroed here; the caller fills rows [0, n) and syncs first.
-template <typename T, int L1, int L2, int SIGN>
-__device__ __forceinline__ void fft4_bluestein(C2<T> *X, int B, const FFT4Desc &d) {
+// ---- Bluestein over L = L1*L2: natural rows [0, n) in, natural rows [0, n) out -------------------
+// Rows [n, L) are never read.  The caller fills rows [0, n) and syncs first.  The direction
+// (sign) only selects the chirp's conjugation and the filter table: the inner four-step
+// transforms are the same for both, so one body serves both directions.
+template <typename T, int L1, int L2>
+__device__ __forceinline__ void fft4_bluestein_body(C2<T> *X, int B, const FFT4Desc &d, int sign) {
     const C2<T> *tw4 = (const C2<T> *)d.tw4;
     const C2<T> *chirp = (const C2<T> *)d.chirp;
-    const C2<T> *filt = (const C2<T> *)(SIGN < 0 ? d.filtf : d.filtb);
+    const C2<T> *filt = (const C2<T> *)(sign < 0 ? d.filtf : d.filtb);
     const int n = d.n;
-    // step A (forward): input * chirp_SIGN
+    const T cs = sign > 0 ? (T)-1 : (T)1;  // chirp_sign = chirp or conj(chirp)
+    // step A (forward): input * chirp_sign
     for (int idx = threadIdx.x; idx < B * L2; idx += blockDim.x) {
         const int c = idx % B, n2 = idx / B;
         C2<T> a[L1];
 #pragma unroll
         for (int n1 = 0; n1 < L1; n1++) {
             const int pos = n2 + L2 * n1;
-            a[n1] = pos < n ? cmul(X[pos * B + c], gtw<T, SIGN>(chirp, pos)) : mk<T>(0, 0);
+            C2<T> w = pos < n ? __ldg(chirp + pos) : mk<T>(0, 0);
+            w.y *= cs;
+            a[n1] = pos < n ? cmul(X[pos * B + c], w) : mk<T>(0, 0);
         }
         dft_reg<T, L1, -1>(a);
 #pragma unroll
@@ -232,7 +237,7 @@ __device__ __forceinline__ void fft4_bluestein(C2<T> *X, int B, const FFT4Desc &
         for (int m2 = 0; m2 < L2; m2++) X[(L2 * k1 + m2) * B + c] = b[m2];
     }
     __syncthreads();
-    // step A' (inverse), output * chirp_SIGN on rows < n
+    // step A' (inverse), output * chirp_sign on rows < n
     for (int idx = threadIdx.x; idx < B * L2; idx += blockDim.x) {
         const int c = idx % B, m2 = idx / B;
         C2<T> a[L1];
@@ -242,10 +247,30 @@ __device__ __forceinline__ void fft4_bluestein(C2<T> *X, int B, const FFT4Desc &
 #pragma unroll
         for (int m1 = 0; m1 < L1; m1++) {
             const int pos = m2 + L2 * m1;
-            if (pos < n) X[pos * B + c] = cmul(a[m1], gtw<T, SIGN>(chirp, pos));
+            if (pos < n) {
+                C2<T> w = __ldg(chirp + pos);
+                w.y *= cs;
+                X[pos * B + c] = cmul(a[m1], w);
+            }
         }
     }
     __syncthreads();
+}
+
+template <typename T, int L1, int L2, int SIGN>
+__device__ __forceinline__ void fft4_bluestein(C2<T> *X, int B, const FFT4Desc &d) {
+    fft4_bluestein_body<T, L1, L2>(X, B, d, SIGN);
+}
+
+// Out-of-line copies for kernels that transform at many call sites (the fused column kernels):
+// one body in the instruction stream instead of one per call site.
+template <typename T, int L1, int L2>
+__device__ __noinline__ void fft4_bluestein_ni(C2<T> *X, int B, const FFT4Desc &d, int sign) {
+    fft4_bluestein_body<T, L1, L2>(X, B, d, sign);
+}
+template <typename T, int L1, int L2, int SIGN>
+__device__ __noinline__ void fft4_np_ni(C2<T> *X, int B, const FFT4Desc &d) {
+    fft4_np<T, L1, L2, SIGN>(X, B, d);
 }
 
 }  // namespace sg

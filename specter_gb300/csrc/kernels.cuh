@@ -36,15 +36,26 @@ struct GenericFFT {
     static __device__ __forceinline__ C2<T> *run(C2<T> *X, C2<T> *Y, int B, const Desc &d, int sign) {
         return fft_exec<T>(X, Y, B, d, sign);
     }
+    // input at rows pos(k), output in natural order
+    static __device__ __forceinline__ C2<T> *run_perm(C2<T> *X, C2<T> *Y, int B, const Desc &d, int sign) {
+        return fft_exec<T>(X, Y, B, d, sign);
+    }
     static __device__ __forceinline__ int pos(int k, const Desc &) { return k; }
 };
 
-template <typename T, int L1, int L2>
+// OUTLINE = true calls the transforms out of line (kernels with many call sites).
+template <typename T, int L1, int L2, bool OUTLINE = false>
 struct FourStep {
     using Desc = FFT4Desc;
     static constexpr int kBuffers = 1;
     static constexpr int kMinBlocks = 2;  // cap registers at 128 so two blocks share an SM
     static __device__ __forceinline__ C2<T> *run(C2<T> *X, C2<T> *, int B, const Desc &d, int sign) {
+        if constexpr (OUTLINE) {
+            if (d.blue) fft4_bluestein_ni<T, L1, L2>(X, B, d, sign);
+            else if (sign < 0) fft4_np_ni<T, L1, L2, -1>(X, B, d);
+            else fft4_np_ni<T, L1, L2, +1>(X, B, d);
+            return X;
+        }
         if (d.blue) {
             if (sign < 0) fft4_bluestein<T, L1, L2, -1>(X, B, d);
             else fft4_bluestein<T, L1, L2, +1>(X, B, d);
@@ -52,6 +63,13 @@ struct FourStep {
             if (sign < 0) fft4_np<T, L1, L2, -1>(X, B, d);
             else fft4_np<T, L1, L2, +1>(X, B, d);
         }
+        return X;
+    }
+    // input at rows pos(k) (permuted unless Bluestein), output in natural order
+    static __device__ __forceinline__ C2<T> *run_perm(C2<T> *X, C2<T> *Y, int B, const Desc &d, int sign) {
+        if (d.blue) return run(X, Y, B, d, sign);
+        if (sign < 0) fft4_pn<T, L1, L2, -1>(X, B, d);
+        else fft4_pn<T, L1, L2, +1>(X, B, d);
         return X;
     }
     static __device__ __forceinline__ int pos(int k, const Desc &d) { return d.blue ? k : perm_pos<L1, L2>(k); }
@@ -232,18 +250,27 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass(Geo g, typen
 
 // ---------------------------------------------------------------------------------
 // x pass helpers: real rows of length nx = 2H through a complex FFT of length H.
+// A block takes RB rows.  Rows move between HBM and shared memory through a staging
+// buffer S[k][r] of row stride SP = RB + 1 (odd, so that both the row-contiguous global
+// side and the column-contiguous shared side run without bank conflicts); the FFT buffer
+// X[pos][r] has stride RB.
 // ---------------------------------------------------------------------------------
 
-// Build Z (H rows, natural order) for a C2R from the half spectrum S (nxh rows, RB columns):
+// Build Z (H rows, natural order) for a C2R from the half spectrum S (nxh rows):
 // Z_k = (X_k + conj X_{H-k}) + i e^{+2 pi i k/nx} (X_k - conj X_{H-k}); Im X_0 = Im X_H = 0.
+// dx = 1 first multiplies the spectrum by i kx (the x derivative).
 template <typename T>
-__device__ __forceinline__ void c2r_pre(const Geo &g, const C2<T> *S, C2<T> *Z, int RB) {
+__device__ __forceinline__ void c2r_pre(const Geo &g, const C2<T> *S, C2<T> *Z, int RB, int SP, int dx = 0) {
     using V = C2<T>;
     const V *xtw = (const V *)g.xtw;
     const int H = g.H;
     for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
         const int k = idx / RB, r = idx % RB;
-        V xk = S[k * RB + r], xm = S[(H - k) * RB + r];
+        V xk = S[k * SP + r], xm = S[(H - k) * SP + r];
+        if (dx) {
+            xk = cimk(g.KX<T>(k), xk);
+            xm = cimk(g.KX<T>(H - k), xm);
+        }
         if (k == 0) { xk.y = 0; xm.y = 0; }
         const V xmc = cconj(xm);
         const V e = cadd(xk, xmc);
@@ -254,19 +281,31 @@ __device__ __forceinline__ void c2r_pre(const Geo &g, const C2<T> *S, C2<T> *Z, 
     }
 }
 
-// From Z = FFT_H(packed real row) (output k at smem row E::pos(k)), write the half spectrum
-// X_0..X_H into S:  X_k = (Z_k + conj Z_{H-k})/2 - (i/2) e^{-2 pi i k/nx} (Z_k - conj Z_{H-k}).
-template <typename T, class E>
-__device__ __forceinline__ void r2c_post(const Geo &g, const typename E::Desc &fd, const C2<T> *Z, C2<T> *S, int RB) {
+// From Z = FFT_H(packed real row), write the half spectrum X_0..X_H into S:
+//   X_k = (Z_k + conj Z_{H-k})/2 - (i/2) e^{-2 pi i k/nx} (Z_k - conj Z_{H-k}).
+// Output k of Z sits at row E::pos(k), or at row k when NAT.
+template <typename T, class E, bool NAT = false>
+__device__ __forceinline__ void r2c_post(const Geo &g, const typename E::Desc &fd, const C2<T> *Z, C2<T> *S, int RB,
+                                         int SP) {
     using V = C2<T>;
     const V *xtw = (const V *)g.xtw;
     const int H = g.H;
     for (int idx = threadIdx.x; idx < (H + 1) * RB; idx += blockDim.x) {
         const int k = idx / RB, r = idx % RB;
-        const V zk = Z[E::pos(k % H, fd) * RB + r], zm = cconj(Z[E::pos((H - k) % H, fd) * RB + r]);
+        const int p0 = NAT ? k % H : E::pos(k % H, fd), p1 = NAT ? (H - k) % H : E::pos((H - k) % H, fd);
+        const V zk = Z[p0 * RB + r], zm = cconj(Z[p1 * RB + r]);
         const V e = cadd(zk, zm), d = csub(zk, zm);
         const V t = cmul(d, __ldg(xtw + k));
-        S[idx] = mk<T>((T)0.5 * (e.x + t.y), (T)0.5 * (e.y - t.x));
+        S[k * SP + r] = mk<T>((T)0.5 * (e.x + t.y), (T)0.5 * (e.y - t.x));
+    }
+}
+
+// shared [rows][SP] staging -> rows of a global array (row stride ld), rows < nv
+template <typename V>
+__device__ __forceinline__ void rows_store(V *out, size_t ld, const V *S, int rows, int SP, int nv) {
+    for (int idx = threadIdx.x; idx < rows * nv; idx += blockDim.x) {
+        const int r = idx / rows, k = idx % rows;
+        out[(size_t)r * ld + k] = S[k * SP + r];
     }
 }
 
@@ -278,31 +317,37 @@ struct XArgs {
     double scale;
 };
 
+// shared memory of the x pass kernels: FFT buffer(s) + staging, for RB rows
+template <class E>
+__host__ __device__ inline size_t x_pass_elems(const typename E::Desc &fd, int nxh, int RB) {
+    return (size_t)E::kBuffers * fd.L * RB + (size_t)nxh * (RB + 1);
+}
+
 template <typename T, class E>
 __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_r2c(Geo g, typename E::Desc fd, XArgs a, int RB) {
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int SP = RB + 1;
     V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * RB, *S = X + (size_t)E::kBuffers * fd.L * RB;
     const int f = blockIdx.z;
     const int row0 = blockIdx.x * RB, nrows = a.nrows * g.ny;
+    const int nv = min(RB, nrows - row0);
     const T *in = (const T *)a.in[f];
     V *out = (V *)a.out[f];
     const int H = g.H;
     // packed real row: element m = (x_{2m}, x_{2m+1})
-    rows_load_async(X, (const V *)(in + (size_t)row0 * g.nx), (size_t)H, H, RB, min(RB, nrows - row0));
+    rows_load_async(S, (const V *)(in + (size_t)row0 * g.nx), (size_t)H, H, RB, nv, SP);
     async_wait();
     __syncthreads();
-    V *R = E::run(X, Y, RB, fd, -1);
-    r2c_post<T, E>(g, fd, R, S, RB);
+    for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) X[idx] = S[(idx / RB) * SP + idx % RB];
     __syncthreads();
-    for (int idx = threadIdx.x; idx < g.nxh * RB; idx += blockDim.x) {
-        const int r = idx / g.nxh, k = idx % g.nxh;
-        if (row0 + r < nrows) {
-            V v = S[k * RB + r];
-            if (a.scale != 1.0) v = cscale(v, (T)a.scale);
-            out[(size_t)(row0 + r) * g.ldx + k] = v;
-        }
-    }
+    V *R = E::run(X, Y, RB, fd, -1);
+    r2c_post<T, E>(g, fd, R, S, RB, SP);
+    __syncthreads();
+    if (a.scale != 1.0)
+        for (int idx = threadIdx.x; idx < g.nxh * SP; idx += blockDim.x) S[idx] = cscale(S[idx], (T)a.scale);
+    __syncthreads();
+    rows_store(out + (size_t)row0 * g.ldx, (size_t)g.ldx, S, g.nxh, SP, nv);
 }
 
 // x pass C2R: r[row] = IFFT_x(in[row]) (Hermitian half spectrum; Im of kx=0, nx/2 ignored)
@@ -310,28 +355,29 @@ template <typename T, class E>
 __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_c2r(Geo g, typename E::Desc fd, XArgs a, int RB) {
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int SP = RB + 1;
     V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * RB, *S = X + (size_t)E::kBuffers * fd.L * RB;
     const int f = blockIdx.z;
     const int row0 = blockIdx.x * RB, nrows = a.nrows * g.ny;
+    const int nv = min(RB, nrows - row0);
     const V *in = (const V *)a.in[f];
     T *out = (T *)a.out[f];
-    rows_load_async(S, in + (size_t)row0 * g.ldx, (size_t)g.ldx, g.nxh, RB, min(RB, nrows - row0));
+    rows_load_async(S, in + (size_t)row0 * g.ldx, (size_t)g.ldx, g.nxh, RB, nv, SP);
     async_wait();
     __syncthreads();
-    c2r_pre<T>(g, S, X, RB);
+    c2r_pre<T>(g, S, X, RB, SP);
     __syncthreads();
     V *R = E::run(X, Y, RB, fd, +1);
     const int H = g.H;
+    const T sc = (T)a.scale;
     for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
-        const int r = idx / H, m = idx % H;
-        if (row0 + r < nrows) {
-            V v = R[E::pos(m, fd) * RB + r];
-            if (a.scale != 1.0) v = cscale(v, (T)a.scale);
-            T *p = out + (size_t)(row0 + r) * g.nx + 2 * m;
-            p[0] = v.x;
-            p[1] = v.y;
-        }
+        const int m = idx / RB, r = idx % RB;
+        V v = R[E::pos(m, fd) * RB + r];
+        if (a.scale != 1.0) v = cscale(v, sc);
+        S[m * SP + r] = v;
     }
+    __syncthreads();
+    rows_store((V *)(out + (size_t)row0 * g.nx), (size_t)H, S, H, SP, nv);
 }
 
 // ---------------------------------------------------------------------------------
@@ -353,56 +399,57 @@ struct XNLArgs {
     double tmp;          // 1/(nx ny nz)^2
 };
 
-// Input t of the x pass: t < 3 velocity rows, then per component u (times i kx), d/dy, d/dz.
+// Input t of the nonlinear x pass: t < 3 the velocity rows; then per component i in [c0, c1)
+// the three rows v_i (to be multiplied by i kx), d/dy v_i, d/dz v_i (term = 0, 1, 2).
 template <typename T>
-__device__ __forceinline__ const C2<T> *xnl_input(const XNLArgs &a, int t, int &dx) {
-    const int nc = a.c1 - a.c0;
-    dx = 0;
-    if (t < 3) return (const C2<T> *)a.u[t];
+__device__ __forceinline__ const C2<T> *xnl_input(const XNLArgs &a, int t, int &term, int &i) {
+    if (t < 3) { term = -1; i = t; return (const C2<T> *)a.u[t]; }
     t -= 3;
-    const int term = t / nc, i = a.c0 + t % nc;
-    if (term == 0) { dx = 1; return (const C2<T> *)a.u[i]; }
-    return (const C2<T> *)(term == 1 ? a.dy[i] : a.dz[i]);
+    term = t % 3;
+    i = a.c0 + t / 3;
+    return (const C2<T> *)(term == 0 ? a.u[i] : term == 1 ? a.dy[i] : a.dz[i]);
 }
 
+// shared memory of k_x_nonlinear: X, S, U[3][H], A[H] for RB rows
+template <class E>
+__host__ __device__ inline size_t x_nl_elems(const typename E::Desc &fd, int nxh, int H, int RB) {
+    return x_pass_elems<E>(fd, nxh, RB) + (size_t)4 * H * RB;
+}
+
+// Components are formed one after another: the three physical velocity rows stay in U, the
+// product accumulates in A, and the last product is formed in place in the FFT buffer, at
+// the permuted positions where the inverse transform left it, so the forward transform
+// starts from permuted input (E::run_perm) and no copy is needed.  Input t+1 is copied into
+// S while input t is transformed.
 template <typename T, class E>
 __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, typename E::Desc fd, XNLArgs a, int RB) {
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int H = g.H, L = fd.L, nxh = g.nxh;
+    const int H = g.H, L = fd.L, nxh = g.nxh, SP = RB + 1;
     V *X = (V *)smem_raw;
     V *Y = X + (size_t)L * RB;
-    V *Sb[2];
-    Sb[0] = X + (size_t)E::kBuffers * L * RB;   // two nxh * RB spectral row stagings (prefetch)
-    Sb[1] = Sb[0] + (size_t)nxh * RB;
-    V *U = Sb[1] + (size_t)nxh * RB;            // 3 * H * RB physical velocity rows
-    V *P = U + (size_t)3 * H * RB;              // H * RB product operand
-    V *A = P + (size_t)H * RB;                  // (c1-c0) * H * RB accumulators
-    const int c0 = a.c0, c1 = a.c1, nc = c1 - c0;
+    V *S = X + (size_t)E::kBuffers * L * RB;   // nxh x SP spectral row staging
+    V *U = S + (size_t)nxh * SP;               // 3 x H x RB physical velocity rows
+    V *A = U + (size_t)3 * H * RB;             // H x RB accumulator
+    const int nc = a.c1 - a.c0;
     const int row0 = blockIdx.x * RB, nrows = a.nrows * g.ny;
     const int nv = min(RB, nrows - row0);
     const int T_in = 3 + 3 * nc;
     const T tmp = (T)a.tmp;
-    int dx;
-    rows_load_async(Sb[0], xnl_input<T>(a, 0, dx) + (size_t)row0 * g.ldx, (size_t)g.ldx, nxh, RB, nv);
+    const size_t off = (size_t)row0 * g.ldx;
+    int term, i;
+    rows_load_async(S, xnl_input<T>(a, 0, term, i) + off, (size_t)g.ldx, nxh, RB, nv, SP);
     for (int t = 0; t < T_in; t++) {
-        V *S = Sb[t & 1];
+        xnl_input<T>(a, t, term, i);
         async_wait();
-        __syncthreads();  // input t is in S; every thread is done with the previous iteration
-        if (t + 1 < T_in) {
-            int dx1;
-            const V *nxt = xnl_input<T>(a, t + 1, dx1);
-            rows_load_async(Sb[(t + 1) & 1], nxt + (size_t)row0 * g.ldx, (size_t)g.ldx, nxh, RB, nv);
+        __syncthreads();  // S holds input t; the previous iteration is complete
+        c2r_pre<T>(g, S, X, RB, SP, term == 0);
+        __syncthreads();  // S is free
+        if (term != 2 && t + 1 < T_in) {
+            int tn, in_;
+            rows_load_async(S, xnl_input<T>(a, t + 1, tn, in_) + off, (size_t)g.ldx, nxh, RB, nv, SP);
         }
-        xnl_input<T>(a, t, dx);
-        if (dx) {
-            for (int idx = threadIdx.x; idx < nxh * RB; idx += blockDim.x) S[idx] = cimk(g.KX<T>(idx / RB), S[idx]);
-            __syncthreads();
-        }
-        c2r_pre<T>(g, S, X, RB);
-        __syncthreads();
         V *R = E::run(X, Y, RB, fd, +1);
-        const int term = t < 3 ? -1 : (t - 3) / nc, i = t < 3 ? t : c0 + (t - 3) % nc;
         if (term < 2) {
             for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
                 const int m = idx / RB, r = idx % RB;
@@ -411,33 +458,29 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, 
                     U[(size_t)i * H * RB + idx] = p;
                 } else if (term == 0) {
                     const V u = U[idx];
-                    A[(size_t)(i - c0) * H * RB + idx] = mk<T>(u.x * p.x, u.y * p.y);
+                    A[idx] = mk<T>(u.x * p.x, u.y * p.y);
                 } else {
                     const V u = U[(size_t)H * RB + idx];
-                    V &acc = A[(size_t)(i - c0) * H * RB + idx];
-                    acc = mk<T>(acc.x + u.x * p.x, acc.y + u.y * p.y);
+                    A[idx] = mk<T>(A[idx].x + u.x * p.x, A[idx].y + u.y * p.y);
                 }
             }
         } else {
-            // term 3: (acc + u_z d/dz v_i) * tmp, forward R2C, store
+            // (acc + u_z d/dz v_i) * tmp in place, forward transform from permuted order, R2C
             for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
                 const int m = idx / RB, r = idx % RB;
-                P[idx] = R[E::pos(m, fd) * RB + r];
+                const int q = E::pos(m, fd) * RB + r;
+                const V u = U[(size_t)2 * H * RB + idx], p = R[q], acc = A[idx];
+                R[q] = mk<T>((acc.x + u.x * p.x) * tmp, (acc.y + u.y * p.y) * tmp);
             }
             __syncthreads();
-            for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
-                const V u = U[(size_t)2 * H * RB + idx], p = P[idx];
-                const V acc = A[(size_t)(i - c0) * H * RB + idx];
-                X[idx] = mk<T>((acc.x + u.x * p.x) * tmp, (acc.y + u.y * p.y) * tmp);
-            }
+            V *Z = E::run_perm(R, R == X ? Y : X, RB, fd, -1);
+            r2c_post<T, E, true>(g, fd, Z, S, RB, SP);
             __syncthreads();
-            R = E::run(X, Y, RB, fd, -1);
-            r2c_post<T, E>(g, fd, R, S, RB);  // S (input t) is consumed: reuse it for the output
-            __syncthreads();
-            V *out = (V *)a.out[i];
-            for (int idx = threadIdx.x; idx < nxh * RB; idx += blockDim.x) {
-                const int r = idx / nxh, k = idx % nxh;
-                if (r < nv) out[(size_t)(row0 + r) * g.ldx + k] = S[k * RB + r];
+            rows_store((V *)a.out[i] + off, (size_t)g.ldx, S, nxh, SP, nv);
+            if (t + 1 < T_in) {
+                __syncthreads();
+                int tn, in_;
+                rows_load_async(S, xnl_input<T>(a, t + 1, tn, in_) + off, (size_t)g.ldx, nxh, RB, nv, SP);
             }
         }
     }

@@ -128,10 +128,11 @@ static int launch_y(Plan &P, const YArgs &a0, int nf, int nplanes) {
 template <typename T>
 static int launch_x(Plan &P, const XArgs &a, int nf, bool r2c) {
     const size_t es = sizeof(C2<T>);
-    const size_t per = (2 * (size_t)P.tx.d.L + P.nxh) * es;
-    const int rb = pick_tile(per);
+    int rb = 0;
+    for (int t : {16, 8, 4, 2, 1})
+        if (x_pass_elems<GenericFFT<T>>(P.tx.d, P.nxh, t) * es <= kSmemBudget) { rb = t; break; }
     if (!rb) { set_error("x length too large for shared memory"); return ERR_SHAPE; }
-    const size_t sm = per * rb;
+    const size_t sm = x_pass_elems<GenericFFT<T>>(P.tx.d, P.nxh, rb) * es;
     const dim3 grid(cdiv(a.nrows * P.ny, rb), 1, nf);
     const double rows = (double)a.nrows * P.ny;
     const double bytes = nf * rows * ((double)P.nxh * P.elt() + (double)P.nx * P.rel());
@@ -152,10 +153,11 @@ static int launch_x(Plan &P, const XArgs &a, int nf, bool r2c) {
 template <typename T>
 static int launch_x_nl(Plan &P, const XNLArgs &a) {
     const size_t es = sizeof(C2<T>);
-    const size_t per = (2 * (size_t)P.tx.d.L + 2 * (size_t)P.nxh + (4 + (a.c1 - a.c0)) * (size_t)P.H) * es;
-    const int rb = pick_tile(per);
+    int rb = 0;
+    for (int t : {16, 8, 4, 2, 1})
+        if (x_nl_elems<GenericFFT<T>>(P.tx.d, P.nxh, P.H, t) * es <= kSmemBudget) { rb = t; break; }
     if (!rb) { set_error("x length too large for shared memory"); return ERR_SHAPE; }
-    const size_t sm = per * rb;
+    const size_t sm = x_nl_elems<GenericFFT<T>>(P.tx.d, P.nxh, P.H, rb) * es;
     const int nc = a.c1 - a.c0;
     // rows read: 3 velocity rows (+ theta), d/dy and d/dz rows of each component; written: NL rows
     const double nin = 3 + (a.c1 == 4 ? 1 : 0) + 2 * nc;
