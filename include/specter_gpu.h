@@ -49,6 +49,8 @@ int specter_version(void);
 int specter_device_count(int *count);
 /* selects the CUDA device used by plans created afterwards on the calling thread */
 int specter_set_device(int device);
+/* free and total device memory of the current device (admission by memory budget) */
+int specter_device_memory(unsigned long long *free_bytes, unsigned long long *total_bytes);
 
 /* ---- plan: fcgram_create_plan (src/fftp/fcgram_mod.f90:49-144) + grid/kes setup
  *      (src/specter.fpp:683-800).  n = (nx, ny, nz) totals, c = (Cx, Cy, Cz), o = (ox, oy, oz)
@@ -148,6 +150,29 @@ int specter_solver_step(specter_solver *s, int nsteps);      /* rkstep1 + ORD st
 int specter_solver_stage(specter_solver *s, int o);          /* one stage o (rkstep2 body) */
 /* checks the state for non-finite values (SPECTER_ERR_NONFINITE if any) */
 int specter_solver_check(specter_solver *s);
+
+/* ---- autotuning and CUDA graphs (no reference counterpart: the ensemble and serving forms).
+ * specter_solver_autotune times RK steps of the solver for each tile-width cap of the z, y, x
+ *      and fused kernel families and keeps the fastest cap per family in the solver's plan; the
+ *      state is restored afterwards.  caps (optional, 4 ints) receives the chosen caps.
+ * specter_plan_tile_caps sets the caps directly (entries <= 0 leave a cap unchanged).
+ * specter_graph_create captures nsteps RK steps of n solvers into one CUDA graph: each
+ *      solver's kernels stay on its plan stream, the chains of different plans are parallel
+ *      branches.  specter_graph_launch runs it, ordered after the work already queued on those
+ *      plan streams and before work queued on them afterwards.  The solvers' own state fields
+ *      are advanced in place.  Destroy a graph before its solvers. */
+typedef struct specter_graph specter_graph;
+int specter_solver_autotune(specter_solver *s, int caps[4]);
+int specter_plan_tile_caps(specter_plan *plan, const int caps[4]);
+int specter_graph_create(specter_solver *const *solvers, int n, int nsteps, specter_graph **out);
+int specter_graph_launch(specter_graph *g);
+int specter_graph_synchronize(specter_graph *g);
+int specter_graph_kernels(specter_graph *g, long long *kernels);  /* kernels per launch */
+int specter_graph_query(specter_graph *g, int *done);  /* 1 when every launch so far has finished */
+/* device bytes held by the solver: its state, RK and fused-stage buffers and its plan (tables
+ * and the scratch fields allocated so far) */
+int specter_solver_memory(specter_solver *s, unsigned long long *bytes);
+int specter_graph_destroy(specter_graph *g);
 
 /* ---- timers: out = {ffttime, tratime, comtime, conttime, tottime, stages} in seconds,
  *      accumulated from CUDA events (the reference's fftp_mod.fpp:32-37 accumulators) */

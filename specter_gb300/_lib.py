@@ -31,6 +31,9 @@ EXPORTS = [
     "specter_s_imposebc",
     "specter_solver_create", "specter_solver_destroy", "specter_solver_fields", "specter_solver_step",
     "specter_solver_stage", "specter_solver_check",
+    "specter_solver_autotune", "specter_plan_tile_caps",
+    "specter_graph_create", "specter_graph_launch", "specter_graph_synchronize", "specter_graph_kernels",
+    "specter_graph_destroy", "specter_graph_query", "specter_solver_memory", "specter_device_memory",
     "specter_timers", "specter_timers_reset",
     "specter_profile", "specter_profile_report", "specter_launch_count",
 ]
@@ -83,6 +86,16 @@ def load(path: str | None = None):
     L.specter_solver_create.argtypes = [VP, C.POINTER(SolverParams), C.POINTER(VP)]
     L.specter_solver_step.argtypes = [VP, C.c_int]
     L.specter_solver_stage.argtypes = [VP, C.c_int]
+    L.specter_solver_autotune.argtypes = [VP, C.POINTER(C.c_int)]
+    L.specter_plan_tile_caps.argtypes = [VP, C.POINTER(C.c_int)]
+    L.specter_graph_create.argtypes = [C.POINTER(VP), C.c_int, C.c_int, C.POINTER(VP)]
+    L.specter_graph_launch.argtypes = [VP]
+    L.specter_graph_synchronize.argtypes = [VP]
+    L.specter_graph_kernels.argtypes = [VP, C.POINTER(C.c_longlong)]
+    L.specter_graph_destroy.argtypes = [VP]
+    L.specter_graph_query.argtypes = [VP, C.POINTER(C.c_int)]
+    L.specter_solver_memory.argtypes = [VP, C.POINTER(C.c_ulonglong)]
+    L.specter_device_memory.argtypes = [C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]
     L.specter_field_create.argtypes = [VP, C.c_int, C.POINTER(VP)]
     L.specter_field_upload.argtypes = [VP, VP]
     L.specter_field_download.argtypes = [VP, VP]

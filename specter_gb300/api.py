@@ -354,5 +354,73 @@ class Solver:
     def check(self):
         check(_L(self.plan).specter_solver_check(self.h))
 
+    def autotune(self):
+        """Pick the tile-width caps of the plan's kernel families by timing RK steps of this
+        solver (state restored).  Returns the caps (z, y, x, fused)."""
+        caps = (C.c_int * 4)()
+        check(_L(self.plan).specter_solver_autotune(self.h, caps))
+        return tuple(caps)
+
+
+def device_memory():
+    """(free, total) bytes of the current device."""
+    f, t = C.c_ulonglong(), C.c_ulonglong()
+    check(load().specter_device_memory(C.byref(f), C.byref(t)))
+    return f.value, t.value
+
+
+def solver_memory(s: "Solver") -> int:
+    """Device bytes held by a solver (state, RK and fused buffers, its plan's tables and scratch)."""
+    b = C.c_ulonglong()
+    check(_L(s.plan).specter_solver_memory(s.h, C.byref(b)))
+    return b.value
+
+
+def set_tile_caps(plan: Plan, caps):
+    """Tile-width caps (z, y, x, fused) of the plan's kernels; entries <= 0 are left unchanged."""
+    c = (C.c_int * 4)(*caps)
+    check(_L(plan).specter_plan_tile_caps(plan.h, c))
+
+
+class Graph:
+    """nsteps RK steps of several solvers captured as one CUDA graph (specter_graph_create):
+    each solver's kernels on its own plan stream, the solvers as parallel branches."""
+
+    def __init__(self, solvers, nsteps=1):
+        self.solvers = list(solvers)
+        L = load()
+        self._L = L
+        arr = (C.c_void_p * len(self.solvers))(*[s.h.value for s in self.solvers])
+        h = C.c_void_p()
+        check(L.specter_graph_create(arr, len(self.solvers), int(nsteps), C.byref(h)))
+        self.h = h
+        self.nsteps = nsteps
+        n = C.c_longlong()
+        check(L.specter_graph_kernels(h, C.byref(n)))
+        self.kernels = n.value
+
+    def launch(self):
+        check(self._L.specter_graph_launch(self.h))
+
+    def done(self) -> bool:
+        """True when every launch so far has finished (non-blocking)."""
+        d = C.c_int()
+        check(self._L.specter_graph_query(self.h, C.byref(d)))
+        return bool(d.value)
+
+    def synchronize(self):
+        check(self._L.specter_graph_synchronize(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.specter_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
 
 __all__ = [n for n in dir() if not n.startswith("_")] + ["SpecterError"]

@@ -2,6 +2,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <string>
 #include <vector>
 
 #include "../../include/specter_gpu.h"
@@ -80,6 +81,16 @@ int specter_device_count(int *count) {
     cudaError_t e = cudaGetDeviceCount(&n);
     if (e != cudaSuccess) { *count = 0; set_error(cudaGetErrorString(e)); return SPECTER_ERR_CUDA; }
     *count = n;
+    return SPECTER_OK;
+}
+
+int specter_device_memory(unsigned long long *free_bytes, unsigned long long *total_bytes) {
+    if (!free_bytes || !total_bytes) { set_error("null argument"); return SPECTER_ERR_ARG; }
+    size_t f = 0, t = 0;
+    cudaError_t e = cudaMemGetInfo(&f, &t);
+    if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); return SPECTER_ERR_CUDA; }
+    *free_bytes = f;
+    *total_bytes = t;
     return SPECTER_OK;
 }
 
@@ -512,6 +523,228 @@ int specter_solver_check(specter_solver *s) {
         if (st) return st;
         if (!(e == e) || e > 1e300) { set_error("non-finite value in the solver state"); return SPECTER_ERR_NONFINITE; }
     }
+    return SPECTER_OK;
+}
+
+// ------------------------------------------------------------------ autotuning, graphs
+
+}  // extern "C"
+
+// Device copies of a solver's state (velocity, theta, pressure) around trial steps.
+struct StateCopy {
+    std::vector<std::pair<void *, void *>> pairs;  // (state field, copy)
+    int take(specter_solver *s) {
+        Plan &P = *s->plan->p;
+        specter_field *f[5] = {s->v[0], s->v[1], s->v[2], s->v[3], s->pr};
+        for (specter_field *x : f) {
+            if (!x) continue;
+            void *c = nullptr;
+            if (cudaMalloc(&c, x->bytes) != cudaSuccess) { cudaGetLastError(); release(); set_error("cudaMalloc failed"); return SPECTER_ERR_OOM; }
+            cudaMemcpyAsync(c, x->d, x->bytes, cudaMemcpyDeviceToDevice, P.stream);
+            pairs.push_back({x->d, c});
+        }
+        return check_launch("state copy");
+    }
+    int put_back(specter_solver *s) {
+        Plan &P = *s->plan->p;
+        size_t i = 0;
+        specter_field *f[5] = {s->v[0], s->v[1], s->v[2], s->v[3], s->pr};
+        for (specter_field *x : f) {
+            if (!x) continue;
+            cudaMemcpyAsync(pairs[i].first, pairs[i].second, x->bytes, cudaMemcpyDeviceToDevice, P.stream);
+            i++;
+        }
+        cudaStreamSynchronize(P.stream);
+        return check_launch("state restore");
+    }
+    void release() {
+        for (auto &p : pairs) cudaFree(p.second);
+        pairs.clear();
+    }
+};
+
+extern "C" {
+
+int specter_plan_tile_caps(specter_plan *plan, const int caps[4]) {
+    CHECK_PLAN(plan);
+    if (!caps) { set_error("null argument"); return SPECTER_ERR_ARG; }
+    for (int i = 0; i < 4; i++)
+        if (caps[i] > 0) plan->p->tile_cap[i] = caps[i];
+    return SPECTER_OK;
+}
+
+int specter_solver_autotune(specter_solver *s, int caps[4]) {
+    if (!s) { set_error("null solver"); return SPECTER_ERR_ARG; }
+    Plan &P = *s->plan->p;
+    if (P.profile) { set_error("autotune with profiling enabled"); return SPECTER_ERR_STATE; }
+    StateCopy snap;
+    int st = snap.take(s);
+    if (st) return st;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    // time of two RK steps after one warm-up step at the current caps (infinite on error)
+    auto trial = [&]() -> float {
+        if (specter_solver_step(s, 1)) { cudaGetLastError(); return 1e30f; }
+        cudaEventRecord(e0, P.stream);
+        if (specter_solver_step(s, 2)) { cudaGetLastError(); return 1e30f; }
+        cudaEventRecord(e1, P.stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) { cudaGetLastError(); return 1e30f; }
+        float ms = 1e30f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        return ms;
+    };
+    for (int kind = 0; kind < 4; kind++) {
+        int best = P.tile_cap[kind];
+        float best_ms = trial();
+        for (int cap : {16, 8, 4, 2}) {
+            if (cap == best) continue;
+            P.tile_cap[kind] = cap;
+            const float ms = trial();
+            if (ms < best_ms) { best_ms = ms; best = cap; }
+        }
+        P.tile_cap[kind] = best;
+        // the state was advanced by the trials: bring it back before the next family
+        if ((st = snap.put_back(s))) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!st) st = snap.put_back(s);
+    snap.release();
+    if (!st && caps)
+        for (int i = 0; i < 4; i++) caps[i] = P.tile_cap[i];
+    return st;
+}
+
+}  // extern "C"
+
+struct specter_graph {
+    cudaStream_t root = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<cudaStream_t> streams;  // distinct plan streams of the captured solvers
+    std::vector<cudaEvent_t> ev;        // one per stream (join at capture, entry at launch)
+    cudaEvent_t fork = nullptr, done = nullptr;
+    long long kernels = 0;
+};
+
+extern "C" {
+
+int specter_graph_destroy(specter_graph *g) {
+    if (!g) return SPECTER_OK;
+    if (g->root) cudaStreamSynchronize(g->root);
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    for (cudaEvent_t e : g->ev) cudaEventDestroy(e);
+    if (g->fork) cudaEventDestroy(g->fork);
+    if (g->done) cudaEventDestroy(g->done);
+    if (g->root) cudaStreamDestroy(g->root);
+    delete g;
+    return SPECTER_OK;
+}
+
+int specter_graph_create(specter_solver *const *solvers, int n, int nsteps, specter_graph **out) {
+    if (!solvers || n < 1 || nsteps < 1 || !out) { set_error("bad graph arguments"); return SPECTER_ERR_ARG; }
+    *out = nullptr;
+    for (int i = 0; i < n; i++) {
+        if (!solvers[i]) { set_error("null solver"); return SPECTER_ERR_ARG; }
+        if (solvers[i]->plan->p->profile) { set_error("graph capture with profiling enabled"); return SPECTER_ERR_STATE; }
+    }
+    // one trial step per solver (state restored) creates every lazily allocated buffer and
+    // uploads every table, so that the capture records kernels and copies only
+    for (int i = 0; i < n; i++) {
+        StateCopy snap;
+        int st = snap.take(solvers[i]);
+        if (!st) st = specter_solver_step(solvers[i], 1);
+        if (!st) st = snap.put_back(solvers[i]);
+        snap.release();
+        if (st) return st;
+    }
+    specter_graph *g = new specter_graph();
+    for (int i = 0; i < n; i++) {
+        cudaStream_t s = solvers[i]->plan->p->stream;
+        bool seen = false;
+        for (cudaStream_t t : g->streams) seen = seen || t == s;
+        if (!seen) g->streams.push_back(s);
+    }
+    cudaStreamCreateWithFlags(&g->root, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&g->fork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming);
+    g->ev.resize(g->streams.size());
+    for (auto &e : g->ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    int st = SPECTER_OK;
+    if (cudaStreamBeginCapture(g->root, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+        st = check_launch("graph capture");
+        specter_graph_destroy(g);
+        return st ? st : SPECTER_ERR_CUDA;
+    }
+    cudaEventRecord(g->fork, g->root);
+    for (cudaStream_t s : g->streams) cudaStreamWaitEvent(s, g->fork, 0);
+    for (int i = 0; i < n && !st; i++) {
+        Plan &P = *solvers[i]->plan->p;
+        const long long l0 = P.launches;
+        st = specter_solver_step(solvers[i], nsteps);
+        g->kernels += P.launches - l0;
+    }
+    for (size_t j = 0; j < g->streams.size(); j++) {
+        cudaEventRecord(g->ev[j], g->streams[j]);
+        cudaStreamWaitEvent(g->root, g->ev[j], 0);
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(g->root, &graph);
+    g->graph = graph;
+    if (!st && ec != cudaSuccess) { set_error(std::string("graph capture: ") + cudaGetErrorString(ec)); st = SPECTER_ERR_CUDA; }
+    if (!st && cudaGraphInstantiate(&g->exec, g->graph, 0) != cudaSuccess) {
+        set_error("graph instantiation failed");
+        st = SPECTER_ERR_CUDA;
+    }
+    cudaGetLastError();
+    if (st) { specter_graph_destroy(g); return st; }
+    *out = g;
+    return SPECTER_OK;
+}
+
+int specter_graph_launch(specter_graph *g) {
+    if (!g || !g->exec) { set_error("null graph"); return SPECTER_ERR_ARG; }
+    for (size_t j = 0; j < g->streams.size(); j++) {
+        cudaEventRecord(g->ev[j], g->streams[j]);
+        cudaStreamWaitEvent(g->root, g->ev[j], 0);
+    }
+    if (cudaGraphLaunch(g->exec, g->root) != cudaSuccess) return check_launch("graph launch");
+    cudaEventRecord(g->done, g->root);
+    for (cudaStream_t s : g->streams) cudaStreamWaitEvent(s, g->done, 0);
+    return check_launch("graph launch");
+}
+
+int specter_graph_synchronize(specter_graph *g) {
+    if (!g) { set_error("null graph"); return SPECTER_ERR_ARG; }
+    if (cudaStreamSynchronize(g->root) != cudaSuccess) return check_launch("graph synchronize");
+    return SPECTER_OK;
+}
+
+int specter_graph_query(specter_graph *g, int *done) {
+    if (!g || !done) { set_error("null argument"); return SPECTER_ERR_ARG; }
+    const cudaError_t e = cudaStreamQuery(g->root);
+    if (e == cudaSuccess) { *done = 1; return SPECTER_OK; }
+    if (e == cudaErrorNotReady) { cudaGetLastError(); *done = 0; return SPECTER_OK; }
+    return check_launch("graph query");
+}
+
+int specter_solver_memory(specter_solver *s, unsigned long long *bytes) {
+    if (!s || !bytes) { set_error("null argument"); return SPECTER_ERR_ARG; }
+    const Plan &P = *s->plan->p;
+    const int nc = s->sp.solver == SPECTER_BOUSS ? 4 : 3;
+    unsigned long long b = 0;
+    b += (unsigned long long)(2 * nc + 1) * P.field_bytes();  // state, pr, RK start
+    b += fused_bytes(P, s->fs);
+    b += plan_bytes(P);
+    *bytes = b;
+    return SPECTER_OK;
+}
+
+int specter_graph_kernels(specter_graph *g, long long *kernels) {
+    if (!g || !kernels) { set_error("null argument"); return SPECTER_ERR_ARG; }
+    *kernels = g->kernels;
     return SPECTER_OK;
 }
 

@@ -33,6 +33,9 @@ template <typename V> __device__ __forceinline__ V cmuli(V a, int s) {
 }
 
 __host__ __device__ __forceinline__ int cdiv(int a, int b) { return (a + b - 1) / b; }
+// log2 of a power of two.  Tile widths (kx columns per z/y tile, rows per x tile, FFT batch
+// widths) are powers of two, so index splits use shifts and masks instead of divisions.
+__device__ __forceinline__ int lg2(int pow2) { return __ffs(pow2) - 1; }
 
 // ---- asynchronous global -> shared copies (cp.async): the copies of a whole tile are in
 // flight together; async_wait() completes them for the calling thread (a barrier follows).
@@ -55,8 +58,9 @@ __device__ __forceinline__ void async_wait_n() { asm volatile("cp.async.wait_gro
 // __syncthreads() before reading the tile.
 template <typename V>
 __device__ __forceinline__ void tile_load_async(V *dst, const V *src, size_t stride, int rows, int TK, int nv) {
+    const int lgTK = lg2(TK);
     for (int idx = threadIdx.x; idx < rows * TK; idx += blockDim.x) {
-        const int k = idx / TK, c = idx % TK;
+        const int k = idx >> lgTK, c = idx & (TK - 1);
         if (c < nv) cp_async<sizeof(V)>(dst + idx, src + (size_t)k * stride + c);
         else { V z; z.x = 0; z.y = 0; dst[idx] = z; }
     }
@@ -69,10 +73,15 @@ __device__ __forceinline__ void tile_load_async(V *dst, const V *src, size_t str
 template <typename V>
 __device__ __forceinline__ void rows_load_async(V *dst, const V *src, size_t cstride, int rows, int TK, int nv,
                                                 int dstride) {
+    // (c, k) = divmod(idx, rows), advanced by blockDim.x without dividing per element
+    const int sc = blockDim.x / rows, sk = blockDim.x - sc * rows;
+    int c = threadIdx.x / rows, k = threadIdx.x - c * rows;
     for (int idx = threadIdx.x; idx < rows * TK; idx += blockDim.x) {
-        const int c = idx / rows, k = idx % rows;
         if (c < nv) cp_async<sizeof(V)>(dst + k * dstride + c, src + (size_t)c * cstride + k);
         else { V z; z.x = 0; z.y = 0; dst[k * dstride + c] = z; }
+        c += sc;
+        k += sk;
+        if (k >= rows) { k -= rows; c++; }
     }
     async_commit();
 }

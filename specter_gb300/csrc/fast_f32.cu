@@ -148,7 +148,7 @@ int zinv(Plan &P, const ZInvArgs &a0, int nf, double bytes) {
     ZInvArgs a = a0;
     a.staged = stage_tile(a.out0, a.out1, nf, P.tz4.d.L, P.nz);
     const size_t per = ((size_t)P.tz4.d.L + (a.staged ? P.nz : 0)) * sizeof(float2);
-    const int tk = pick(per);
+    const int tk = P.capped(pick(per), Plan::kTileZ);
     const size_t sm = per * tk;
     smem_attr(k_z_inverse<float, E>, sm);
     Scope s(P, "z_inverse", bytes);
@@ -159,7 +159,7 @@ int zinv(Plan &P, const ZInvArgs &a0, int nf, double bytes) {
 template <int L1, int L2>
 int zfwd(Plan &P, const ZFwdArgs &a, int nf, double bytes) {
     using E = FourStep<float, L1, L2>;
-    const int tk = pick((size_t)P.tz4.d.L * sizeof(float2));
+    const int tk = P.capped(pick((size_t)P.tz4.d.L * sizeof(float2)), Plan::kTileZ);
     const size_t sm = (size_t)P.tz4.d.L * tk * sizeof(float2);
     smem_attr(k_z_forward<float, E>, sm);
     Scope s(P, "z_forward", bytes);
@@ -173,7 +173,7 @@ int ypass(Plan &P, const YArgs &a0, int nf, int nplanes, double bytes) {
     YArgs a = a0;
     a.staged = stage_tile(a.out0, a.out1, nf, P.ty4.d.L, P.ny);
     const size_t per = ((size_t)P.ty4.d.L + (a.staged ? P.ny : 0)) * sizeof(float2);
-    const int tk = pick(per);
+    const int tk = P.capped(pick(per), Plan::kTileY);
     const size_t sm = per * tk;
     smem_attr(k_y_pass<float, E>, sm);
     Scope s(P, a.sign < 0 ? "y_forward" : "y_inverse", bytes);
@@ -186,7 +186,7 @@ int xpass(Plan &P, const XArgs &a, int nf, bool r2c, double bytes) {
     using E = FourStep<float, L1, L2>;
     int rb = 0;
     for (int t : {16, 8, 4, 2, 1})
-        if (x_pass_elems<E>(P.tx4.d, P.nxh, t) * sizeof(float2) <= kFastBudget) { rb = t; break; }
+        if (t <= P.tile_cap[Plan::kTileX] && x_pass_elems<E>(P.tx4.d, P.nxh, t) * sizeof(float2) <= kFastBudget) { rb = t; break; }
     if (!rb) return kNoFast;
     const size_t sm = x_pass_elems<E>(P.tx4.d, P.nxh, rb) * sizeof(float2);
     const dim3 grid(cdiv(a.nrows * P.ny, rb), 1, nf);
@@ -207,7 +207,7 @@ int xnl(Plan &P, const XNLArgs &a, double bytes) {
     using E = FourStep<float, L1, L2>;
     int rb = 0;
     for (int t : {16, 8, 4, 2, 1})
-        if (x_nl_elems<E>(P.tx4.d, P.nxh, P.H, t) * sizeof(float2) <= kMaxSmem) { rb = t; break; }
+        if (t <= P.tile_cap[Plan::kTileX] && x_nl_elems<E>(P.tx4.d, P.nxh, P.H, t) * sizeof(float2) <= kMaxSmem) { rb = t; break; }
     if (!rb) return kNoFast;
     const size_t sm = x_nl_elems<E>(P.tx4.d, P.nxh, P.H, rb) * sizeof(float2);
     smem_attr(k_x_nonlinear<float, E>, sm);

@@ -96,9 +96,9 @@ template <typename T, int R>
 __device__ __forceinline__ void stockham_stage(const C2<T> *__restrict__ X, C2<T> *__restrict__ Y, int B, int L,
                                                int Ns, int sign, const C2<T> *tw) {
     const int nR = L / R, step = L / (Ns * R);
-    const int total = B * nR;
+    const int total = B * nR, lgB = lg2(B);
     for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-        const int c = idx % B, j = idx / B;
+        const int c = idx & (B - 1), j = idx >> lgB;
         const int k = j % Ns;
         C2<T> a[R];
 #pragma unroll
@@ -146,19 +146,19 @@ __device__ __noinline__ C2<T> *fft_exec(C2<T> *X, C2<T> *Y, int B, const FFTDesc
     if (!d.blue) return stockham<T>(X, Y, B, d, sign);
     const C2<T> *chirp = (const C2<T> *)d.chirp;
     const C2<T> *filt = (const C2<T> *)(sign < 0 ? d.filtf : d.filtb);
-    const int n = d.n, L = d.L;
+    const int n = d.n, L = d.L, lgB = lg2(B);
     for (int idx = threadIdx.x; idx < L * B; idx += blockDim.x) {
-        const int k = idx / B;
+        const int k = idx >> lgB;
         if (k < n) X[idx] = cmul(X[idx], tw_at<T>(chirp, k, sign));
         else X[idx] = mk<T>(0, 0);
     }
     __syncthreads();
     C2<T> *R = stockham<T>(X, Y, B, d, -1);
-    for (int idx = threadIdx.x; idx < L * B; idx += blockDim.x) R[idx] = cmul(R[idx], __ldg(filt + idx / B));
+    for (int idx = threadIdx.x; idx < L * B; idx += blockDim.x) R[idx] = cmul(R[idx], __ldg(filt + (idx >> lgB)));
     __syncthreads();
     C2<T> *O = (R == X) ? Y : X;
     R = stockham<T>(R, O, B, d, +1);
-    for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) R[idx] = cmul(R[idx], tw_at<T>(chirp, idx / B, sign));
+    for (int idx = threadIdx.x; idx < n * B; idx += blockDim.x) R[idx] = cmul(R[idx], tw_at<T>(chirp, idx >> lgB, sign));
     __syncthreads();
     return R;
 }

@@ -133,10 +133,11 @@ __device__ __forceinline__ C2<T> gtw(const C2<T> *tw, int t) {
 // ---- natural -> permuted (steps A, B) ---------------------------------------------------------
 template <typename T, int L1, int L2, int SIGN>
 __device__ __forceinline__ void fft4_np(C2<T> *X, int B, const FFT4Desc &d) {
+    const int lgB = lg2(B);
     constexpr int L = L1 * L2;
     const C2<T> *tw4 = (const C2<T> *)d.tw4;
     for (int idx = threadIdx.x; idx < B * L2; idx += blockDim.x) {
-        const int c = idx % B, n2 = idx / B;
+        const int c = idx & (B - 1), n2 = idx >> lgB;
         C2<T> a[L1];
 #pragma unroll
         for (int n1 = 0; n1 < L1; n1++) a[n1] = X[(n2 + L2 * n1) * B + c];
@@ -148,7 +149,7 @@ __device__ __forceinline__ void fft4_np(C2<T> *X, int B, const FFT4Desc &d) {
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < B * L1; idx += blockDim.x) {
-        const int c = idx % B, k1 = idx / B;
+        const int c = idx & (B - 1), k1 = idx >> lgB;
         C2<T> b[L2];
 #pragma unroll
         for (int n2 = 0; n2 < L2; n2++) b[n2] = X[(L2 * k1 + n2) * B + c];
@@ -163,9 +164,10 @@ __device__ __forceinline__ void fft4_np(C2<T> *X, int B, const FFT4Desc &d) {
 // ---- permuted -> natural (steps B', A') -------------------------------------------------------
 template <typename T, int L1, int L2, int SIGN>
 __device__ __forceinline__ void fft4_pn(C2<T> *X, int B, const FFT4Desc &d) {
+    const int lgB = lg2(B);
     const C2<T> *tw4 = (const C2<T> *)d.tw4;
     for (int idx = threadIdx.x; idx < B * L1; idx += blockDim.x) {
-        const int c = idx % B, k1 = idx / B;
+        const int c = idx & (B - 1), k1 = idx >> lgB;
         C2<T> b[L2];
 #pragma unroll
         for (int k2 = 0; k2 < L2; k2++) b[k2] = X[(L2 * k1 + k2) * B + c];
@@ -177,7 +179,7 @@ __device__ __forceinline__ void fft4_pn(C2<T> *X, int B, const FFT4Desc &d) {
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < B * L2; idx += blockDim.x) {
-        const int c = idx % B, m2 = idx / B;
+        const int c = idx & (B - 1), m2 = idx >> lgB;
         C2<T> a[L1];
 #pragma unroll
         for (int k1 = 0; k1 < L1; k1++) a[k1] = X[(L2 * k1 + m2) * B + c];
@@ -198,6 +200,7 @@ __device__ __forceinline__ int perm_pos(int k) { return L2 * (k % L1) + k / L1; 
 // transforms are the same for both, so one body serves both directions.
 template <typename T, int L1, int L2>
 __device__ __forceinline__ void fft4_bluestein_body(C2<T> *X, int B, const FFT4Desc &d, int sign) {
+    const int lgB = lg2(B);
     const C2<T> *tw4 = (const C2<T> *)d.tw4;
     const C2<T> *chirp = (const C2<T> *)d.chirp;
     const C2<T> *filt = (const C2<T> *)(sign < 0 ? d.filtf : d.filtb);
@@ -205,7 +208,7 @@ __device__ __forceinline__ void fft4_bluestein_body(C2<T> *X, int B, const FFT4D
     const T cs = sign > 0 ? (T)-1 : (T)1;  // chirp_sign = chirp or conj(chirp)
     // step A (forward): input * chirp_sign
     for (int idx = threadIdx.x; idx < B * L2; idx += blockDim.x) {
-        const int c = idx % B, n2 = idx / B;
+        const int c = idx & (B - 1), n2 = idx >> lgB;
         C2<T> a[L1];
 #pragma unroll
         for (int n1 = 0; n1 < L1; n1++) {
@@ -223,7 +226,7 @@ __device__ __forceinline__ void fft4_bluestein_body(C2<T> *X, int B, const FFT4D
     __syncthreads();
     // step B (forward), filter, step B' (inverse): all in registers
     for (int idx = threadIdx.x; idx < B * L1; idx += blockDim.x) {
-        const int c = idx % B, k1 = idx / B;
+        const int c = idx & (B - 1), k1 = idx >> lgB;
         C2<T> b[L2];
 #pragma unroll
         for (int n2 = 0; n2 < L2; n2++) b[n2] = X[(L2 * k1 + n2) * B + c];
@@ -239,7 +242,7 @@ __device__ __forceinline__ void fft4_bluestein_body(C2<T> *X, int B, const FFT4D
     __syncthreads();
     // step A' (inverse), output * chirp_sign on rows < n
     for (int idx = threadIdx.x; idx < B * L2; idx += blockDim.x) {
-        const int c = idx % B, m2 = idx / B;
+        const int c = idx & (B - 1), m2 = idx >> lgB;
         C2<T> a[L1];
 #pragma unroll
         for (int k1 = 0; k1 < L1; k1++) a[k1] = X[(L2 * k1 + m2) * B + c];

@@ -12,8 +12,89 @@ struct FusedState {
     void *X1[4] = {nullptr, nullptr, nullptr, nullptr};
     void *X2[4] = {nullptr, nullptr, nullptr, nullptr};
     void *side = nullptr;  // theta rows of the kx = 0 and kx = nx/2 columns [2][ny][nzp]
+    void *E[2] = {nullptr, nullptr};  // z spectra of the unit laplace_z profiles, per column
     int nc = 3;
 };
+
+// Unit laplace_z profiles on the physical rows (boundary_mod.fpp:635-675 with c1 = 1, c2 = 0
+// and c1 = 0, c2 = 1): p1 = exp(kh (z - Lz)), p2 = exp(-kh z); for kx = ky = 0, p1 = z, p2 = 1.
+// Rows z >= nzp are zero (the continuation rebuilds them).  FP64.
+__global__ void k_unit_profiles(Geo g, double2 *p1, double2 *p2) {
+    const size_t n = (size_t)g.nz * g.ny * g.ldx;
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const int kx = (int)(q % g.ldx), ky = (int)((q / g.ldx) % g.ny), z = (int)(q / ((size_t)g.ldx * g.ny));
+        double a = 0, b = 0;
+        if (z < g.nzp && kx < g.nxh) {
+            const double zz = g.z[z];
+            if (kx == 0 && ky == 0) {
+                a = zz;
+                b = 1.0;
+            } else {
+                const double kh = sqrt(g.kx[kx] * g.kx[kx] + g.ky[ky] * g.ky[ky]);
+                a = exp(kh * (zz - g.Lz));
+                b = exp(-(kh * zz));
+            }
+        }
+        p1[q] = make_double2(a, 0.0);
+        p2[q] = make_double2(b, 0.0);
+    }
+}
+
+__global__ void k_narrow(const double2 *src, float2 *dst, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
+        dst[q] = make_float2((float)src[q].x, (float)src[q].y);
+}
+
+// The harmonic correction of sol_project forward-transforms a(z) = c1 p1 + c2 p2 and
+// b(z) = da/dz with FC-Gram continuation.  Continuation and transform are linear, so
+// FFT(cont(a)) = c1 E1 + c2 E2 with E_i = FFT(cont(p_i)) fixed by the grid: E1, E2 are computed
+// once here, in FP64 (continuation and transform), and stored in the plan's precision; the
+// column kernel then forms the corrections without transforming.
+static int harmonic_spectra(Plan &P, void *E1, void *E2) {
+    FFTTable t64;
+    const FFTTable *t = &P.tz;
+    if (P.prec != FP64) {
+        if (build_fft_table(t64, P.nz, FP64)) { set_error("FFT table construction failed"); return ERR_CUDA; }
+        t = &t64;
+    }
+    const size_t n = P.field_elems();
+    double2 *buf = nullptr;
+    if (P.prec == FP64) buf = nullptr;
+    else if (cudaMalloc(&buf, 2 * n * sizeof(double2)) != cudaSuccess) {
+        cudaGetLastError();
+        free_fft_table(t64);
+        set_error("out of device memory (harmonic spectra)");
+        return ERR_OOM;
+    }
+    double2 *p1 = P.prec == FP64 ? (double2 *)E1 : buf, *p2 = P.prec == FP64 ? (double2 *)E2 : buf + n;
+    k_unit_profiles<<<152 * 8, 256, 0, P.stream>>>(P.geo, p1, p2);
+    ZFwdArgs a{};
+    a.in[0] = p1; a.in[1] = p2; a.out[0] = p1; a.out[1] = p2;
+    a.in_scale = 1.0;
+    const size_t es = sizeof(double2);
+    int tk = 0;
+    for (int c : {16, 8, 4, 2, 1})
+        if (2 * (size_t)t->d.L * c * es <= 200 * 1024) { tk = c; break; }
+    int st = OK;
+    if (!tk) { set_error("z length too large for shared memory"); st = ERR_SHAPE; }
+    else {
+        const size_t sm = 2 * (size_t)t->d.L * tk * es;
+        auto k = k_z_forward<double, GenericFFT<double>>;
+        if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k<<<dim3(cdiv(P.nxh, tk), P.ny, 2), kThreads, sm, P.stream>>>(P.geo, t->d, a, tk);
+        if (P.prec != FP64) {
+            k_narrow<<<152 * 8, 256, 0, P.stream>>>(p1, (float2 *)E1, n);
+            k_narrow<<<152 * 8, 256, 0, P.stream>>>(p2, (float2 *)E2, n);
+        }
+        if (cudaStreamSynchronize(P.stream) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+            set_error("harmonic spectra: CUDA error");
+            st = ERR_CUDA;
+        }
+    }
+    if (buf) cudaFree(buf);
+    if (P.prec != FP64) free_fft_table(t64);
+    return st;
+}
 
 int fused_create(Plan &P, const StageParams &sp, FusedState **out) {
     *out = nullptr;
@@ -26,14 +107,29 @@ int fused_create(Plan &P, const StageParams &sp, FusedState **out) {
         if (sp.ord >= 3) ok = ok && cudaMalloc(&fs->X2[i], P.field_bytes()) == cudaSuccess;
     }
     if (sp.solver == 1) ok = ok && cudaMalloc(&fs->side, 2 * (size_t)P.ny * P.nzp * P.elt()) == cudaSuccess;
+    for (int i = 0; i < 2; i++) ok = ok && cudaMalloc(&fs->E[i], P.field_bytes()) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         fused_destroy(fs);
         set_error("out of device memory (fused stage buffers)");
         return ERR_OOM;
     }
+    const int st = harmonic_spectra(P, fs->E[0], fs->E[1]);
+    if (st) {
+        fused_destroy(fs);
+        return st;
+    }
     *out = fs;
     return OK;
+}
+
+unsigned long long fused_bytes(const Plan &P, const FusedState *fs) {
+    if (!fs) return 0;
+    unsigned long long b = 0;
+    for (int i = 0; i < 4; i++) b += (fs->X1[i] ? P.field_bytes() : 0) + (fs->X2[i] ? P.field_bytes() : 0);
+    b += fs->side ? 2ull * P.ny * P.nzp * P.elt() : 0;
+    b += (fs->E[0] ? P.field_bytes() : 0) + (fs->E[1] ? P.field_bytes() : 0);
+    return b;
 }
 
 void fused_destroy(FusedState *fs) {
@@ -43,6 +139,8 @@ void fused_destroy(FusedState *fs) {
         if (fs->X2[i]) cudaFree(fs->X2[i]);
     }
     if (fs->side) cudaFree(fs->side);
+    for (int i = 0; i < 2; i++)
+        if (fs->E[i]) cudaFree(fs->E[i]);
     delete fs;
 }
 
@@ -71,6 +169,8 @@ static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], c
     }
     a.pr = pr;
     a.side = fs->side;
+    a.hspec[0] = fs->E[0];
+    a.hspec[1] = fs->E[1];
     a.dt = sp.dt; a.nu = sp.nu; a.kappa = sp.kappa; a.rmp = 1 / (double)o;
     a.xmom = sp.xmom; a.xtemp = sp.xtemp;
     double tmp = 1 / (double)o;
@@ -79,8 +179,9 @@ static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], c
     a.vb[0] = sp.vzsta[0]; a.vb[1] = sp.vzsta[1]; a.vb[2] = sp.vzend[0]; a.vb[3] = sp.vzend[1];
     a.bouss = bouss ? 1 : 0;
     const double row = (double)P.ny * P.nxh * P.elt();
-    // reads: NL (physical rows), vin, cold (+ theta for buoyancy); writes: vout and pr rows
-    const double bv = row * (3.0 * P.nzp + (6.0 + (bouss ? 1 : 0)) * P.nz + 3.0 * P.nz + P.nzp);
+    // reads: NL (physical rows), vin, cold (+ theta for buoyancy), the two unit-profile
+    // spectra; writes: vout and pr rows
+    const double bv = row * (3.0 * P.nzp + (6.0 + (bouss ? 1 : 0) + 2.0) * P.nz + 3.0 * P.nz + P.nzp);
     if ((st = launch<T>(P, a, kFusedVelocity, bv))) return st;
     if (bouss) {
         const double bt = row * (1.0 * P.nzp + 3.0 * P.nz + 1.0 * P.nz);

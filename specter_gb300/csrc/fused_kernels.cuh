@@ -9,7 +9,8 @@
 //              v_imposebc_and_project (vboundary.f90:67-151): z-inverse, no-slip wall planes
 //              from the previous stage's pressure, z-forward with continuation, and sol_project
 //              (boundary_mod.fpp:197-402): Poisson, wall values, laplace_z coefficients (FP64),
-//              pressure, harmonic correction (profiles continued in FP64, then transformed).
+//              pressure, harmonic correction (from the per-column spectra of the two unit
+//              profiles, computed once per plan in FP64: the correction is linear in c1, c2).
 //   scalar:    NL forward, heat current, filter, update, s_imposebc (sboundary.f90:67-165),
 //              fc_filter and the c2r -> /N -> r2c round trip (bouss_rkstep2.f90:56-59).  That
 //              round trip is, exactly, z-inverse, 1/nz, Hermitian symmetrisation of the kx = 0
@@ -29,46 +30,12 @@ struct FusedArgs {
     void *vout[4];        // stage output state
     void *pr;             // pressure potential (mixed), walls read, rows [0, nzp) written
     void *side;           // theta rows of the kx = 0 and kx = nx/2 columns: [2][ny][nzp]
+    const void *hspec[2]; // E1, E2: z spectra (with continuation) of the unit laplace_z profiles
     double dt, nu, kappa, rmp, xmom, xtemp;
     double wall_tmp;      // 1/o, or (o+1)/o when o != ord (noslip_z)
     double vb[4];         // vxzsta, vyzsta, vxzend, vyzend
     int bouss;
 };
-
-// FC-Gram continuation of rows [nzp, nz) from FP64 values of the first and last d rows.
-// lo(c, j) = row j, hi(c, j) = row nzp - d + j, j < d.
-template <typename T, class LO, class HI>
-__device__ __forceinline__ void fc_continuation_fn(const Geo &g, C2<T> *X, int TK, LO lo, HI hi) {
-    const int C = g.cz, d = g.oz, n = g.nz;
-    for (int idx = threadIdx.x; idx < C * TK; idx += blockDim.x) {
-        const int ii = idx / TK, c = idx % TK;
-        double2 t0 = hi(c, 0), b0 = lo(c, d - 1);
-        const double a0 = __ldg(g.dir + ii), a1 = __ldg(g.dir + (C - 1 - ii));
-        double ar = a0 * t0.x + a1 * b0.x, ai = a0 * t0.y + a1 * b0.y;
-        for (int jj = 1; jj < d; jj++) {
-            const double2 t = hi(c, jj), b = lo(c, d - 1 - jj);
-            const double w0 = __ldg(g.dir + ii + C * jj), w1 = __ldg(g.dir + (C - 1 - ii) + C * jj);
-            ar = ar + w0 * t.x + w1 * b.x;
-            ai = ai + w0 * t.y + w1 * b.y;
-        }
-        X[(n - C + ii) * TK + c] = mk<T>((T)ar, (T)ai);
-    }
-}
-
-// laplace_z profile of column (kx, ky) at grid point zz (boundary_mod.fpp:635-675), FP64:
-// a and b = da/dz.  Used for the 2d rows that feed the FC-Gram continuation.
-__device__ __forceinline__ void lap_profile_d(const Geo &g, int kx, int ky, double2 c1, double2 c2, double zz,
-                                              double2 &a, double2 &b) {
-    if (kx == 0 && ky == 0) {
-        a = make_double2(c1.x * zz + c2.x, 0.0);
-        b = make_double2(c1.x, 0.0);
-    } else {
-        const double kh = sqrt(g.kx[kx] * g.kx[kx] + g.ky[ky] * g.ky[ky]);
-        const double e1 = exp(kh * (zz - g.Lz)), e2 = exp(-(kh * zz));
-        a = make_double2(c1.x * e1 + c2.x * e2, c1.y * e1 + c2.y * e2);
-        b = make_double2(kh * (c1.x * e1 - c2.x * e2), kh * (c1.y * e1 - c2.y * e2));
-    }
-}
 
 // Per-column laplace_z parameters in the kernel's precision: kh = |(kx, ky)| and the
 // coefficients c1, c2 (solved in FP64, then rounded); k0 marks the (0, 0) column.
@@ -120,6 +87,7 @@ __device__ __forceinline__ double2 d2(C2<T> v) { return make_double2((double)v.x
 // ----------------------------------------------------------------------------------------------
 template <typename T, class E>
 __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename E::Desc fd, FusedArgs a, int TK) {
+    const int lgTK = lg2(TK);
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nz = g.nz, nzp = g.nzp, L = fd.L;
@@ -131,7 +99,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
     const int kx0 = blockIdx.x * TK, ky = blockIdx.y;
     const int nv = min(TK, g.nxh - kx0);
     auto colq = [&](int z, int c) { return fidx<T>(g, z, ky, kx0 + c); };
-    const T dt = (T)a.dt, nu = (T)a.nu, rmp = (T)a.rmp;
+    const T dt = (T)a.dt, nu = (T)a.nu, rmp = (T)a.rmp, xmom = (T)a.xmom, wall_tmp = (T)a.wall_tmp;
 
     // ---- 1. NL forward transforms, buoyancy, filter, laplak, RK update -> U[c].  Every HBM
     //         read is an asynchronous tile copy: NL_{c+1} (or theta, for the buoyancy of
@@ -165,12 +133,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
         }
         // (a) filtered nonlinear term (minus buoyancy) -> U[c]
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
             V n = mk<T>(0, 0);
             if (c < nv) {
                 const int kx = kx0 + c;
                 n = R[E::pos(k, fd) * TK + c];
-                if (buoy) { const V t = Uc[idx]; n = mk<T>(n.x - (T)a.xmom * t.x, n.y - (T)a.xmom * t.y); }
+                if (buoy) { const V t = Uc[idx]; n = mk<T>(n.x - xmom * t.x, n.y - xmom * t.y); }
                 n = cscale(n, g.FX<T>(kx));
                 n = cscale(n, g.FY<T>(ky));
                 n = cscale(n, g.FZ<T>(k));
@@ -185,7 +153,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
         async_wait();
         __syncthreads();
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
             if (c >= nv) { Uc[idx] = mk<T>(0, 0); continue; }
             const int kx = kx0 + c;
             const T k2 = g.KX<T>(kx) * g.KX<T>(kx) + g.KY<T>(ky) * g.KY<T>(ky) + g.KZ<T>(k) * g.KZ<T>(k);
@@ -205,12 +173,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
         V *R = E::run(X, Y, TK, fd, +1);
         const T inz = (T)1 / (T)nz;
         for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
             V v = cscale(R[E::pos(k, fd) * TK + c], inz);
             if ((k == 0 || k == nzp - 1) && c < nv) {
                 const int kx = kx0 + c;
                 const V p = pr[colq(k, c)];
-                v = cscale(cimk(c3 == 0 ? g.KX<T>(kx) : g.KY<T>(ky), p), (T)a.wall_tmp);
+                v = cscale(cimk(c3 == 0 ? g.KX<T>(kx) : g.KY<T>(ky), p), wall_tmp);
                 if (kx == 0 && ky == 0) v = mk<T>((T)((double)g.nx * g.ny * a.vb[(k == 0 ? 0 : 2) + c3]), (T)0);
             }
             Uc[idx] = v;  // physical rows, natural order (temporary)
@@ -222,18 +190,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
         __syncthreads();
         R = E::run(X, Y, TK, fd, -1);
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
             Uc[idx] = R[E::pos(k, fd) * TK + c];
         }
         __syncthreads();
     }
     // ---- 3. poisson_inhomogeneous: d -> X (natural), v -= i k d, wall sums of vz (FP64)
     const double2 *wtw = (const double2 *)g.wtw;
-    double2 *bnd = coef + 2 * TK;                                 // [TK][2][2d] FP64 profile rows
-    LapCol<T> *lcol = (LapCol<T> *)(bnd + (size_t)TK * 4 * g.oz);  // [TK]
-    const int d = g.oz;
+    LapCol<T> *lcol = (LapCol<T> *)(coef + 2 * TK);  // [TK]
     {
-        const int c = threadIdx.x % TK, k0 = threadIdx.x / TK, kstep = blockDim.x / TK;
+        const int c = threadIdx.x & (TK - 1), k0 = threadIdx.x >> lgTK, kstep = blockDim.x >> lgTK;
         const int kxc = min(kx0 + c, g.nxh - 1);
         const T kx_ = g.KX<T>(kxc), ky_ = g.KY<T>(ky);
         double2 s0 = make_double2(0, 0), s1 = make_double2(0, 0);
@@ -263,7 +229,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
     }
     __syncthreads();
     if (threadIdx.x < TK) {
-        const int c = threadIdx.x, kstep = blockDim.x / TK;
+        const int c = threadIdx.x, kstep = blockDim.x >> lgTK;
         double2 b1 = make_double2(0, 0), b2 = make_double2(0, 0);
         for (int t = 0; t < kstep; t++) {
             const double2 p0 = red[2 * (t * TK + c)], p1 = red[2 * (t * TK + c) + 1];
@@ -284,22 +250,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
         lcol[c] = lc;
     }
     __syncthreads();
-    // ---- 4. pressure: pr = IFFT_z(d)/nz + a(z) on the physical rows; FP64 a, b on the 2d
-    //         rows that feed the continuation of step 5
+    // ---- 4. pressure: pr = IFFT_z(d)/nz + a(z) on the physical rows
     {
-        for (int idx = threadIdx.x; idx < 2 * d * TK; idx += blockDim.x) {
-            const int j = idx / TK, c = idx % TK;
-            const int row = j < d ? j : nzp - 2 * d + j;
-            double2 pa, pb;
-            lap_profile_d(g, min(kx0 + c, g.nxh - 1), ky, coef[2 * c], coef[2 * c + 1], g.z[row], pa, pb);
-            bnd[(c * 2 + 0) * 2 * d + j] = pa;
-            bnd[(c * 2 + 1) * 2 * d + j] = pb;
-        }
         V *R = E::run(X, Y, TK, fd, +1);
         V *prw = (V *)a.pr;
         const T inz = (T)1 / (T)nz, Lz = (T)g.Lz;
         for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
             if (c >= nv) continue;
             V pa, pb;
             lap_profile_t<T>(lcol[c], g.ZZ<T>(k), Lz, pa, pb);
@@ -308,31 +265,33 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
         }
         __syncthreads();
     }
-    // ---- 5. harmonic correction: a and b profiles (bulk rows in the kernel's precision, the
-    //         continuation from the FP64 rows), forward transformed
-    for (int which = 0; which < 2; which++) {
-        const T Lz = (T)g.Lz;
-        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
-            V pa, pb;
-            lap_profile_t<T>(lcol[c], g.ZZ<T>(k), Lz, pa, pb);
-            X[idx] = which == 0 ? pa : pb;
-        }
+    // ---- 5. harmonic correction: the spectra of a = c1 p1 + c2 p2 and b = da/dz are
+    //         c1 E1 + c2 E2 and kh (c1 E1 - c2 E2) (for kx = ky = 0: c1 E1 + c2 E2 and c1 E2,
+    //         real parts of c1, c2), E1, E2 precomputed per column
+    {
+        const V *E1 = (const V *)a.hspec[0], *E2 = (const V *)a.hspec[1];
+        tile_load_async(X, E1 + col0, zs, nz, TK, nv);
+        if (stage2) tile_load_async(X + tile, E2 + col0, zs, nz, TK, nv);
+        async_wait();
         __syncthreads();
-        fc_continuation_fn<T>(g, X, TK, [&](int c, int j) { return bnd[(c * 2 + which) * 2 * d + j]; },
-                              [&](int c, int j) { return bnd[(c * 2 + which) * 2 * d + d + j]; });
-        __syncthreads();
-        V *R = E::run(X, Y, TK, fd, -1);
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
-            const V p = R[E::pos(k, fd) * TK + c];
-            if (which == 0) {
-                const int kx = min(kx0 + c, g.nxh - 1);
-                U[idx] = csub(U[idx], cimk(g.KX<T>(kx), p));
-                U[(size_t)nz * TK + idx] = csub(U[(size_t)nz * TK + idx], cimk(g.KY<T>(ky), p));
+            const int k = idx >> lgTK, c = idx & (TK - 1);
+            if (c >= nv) continue;
+            const LapCol<T> lc = lcol[c];
+            const V e1 = X[idx], e2 = stage2 ? X[tile + idx] : E2[colq(k, c)];
+            V A, B;
+            if (lc.k0) {
+                A = mk<T>(lc.c1.x * e1.x + lc.c2.x * e2.x, lc.c1.x * e1.y + lc.c2.x * e2.y);
+                B = cscale(e2, lc.c1.x);
             } else {
-                U[(size_t)2 * nz * TK + idx] = csub(U[(size_t)2 * nz * TK + idx], p);
+                const V t1 = cmul(lc.c1, e1), t2 = cmul(lc.c2, e2);
+                A = cadd(t1, t2);
+                B = cscale(csub(t1, t2), lc.kh);
             }
+            const int kx = kx0 + c;
+            U[idx] = csub(U[idx], cimk(g.KX<T>(kx), A));
+            U[tile + idx] = csub(U[tile + idx], cimk(g.KY<T>(ky), A));
+            U[2 * tile + idx] = csub(U[2 * tile + idx], B);
         }
         __syncthreads();
     }
@@ -340,7 +299,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
     for (int c3 = 0; c3 < 3; c3++) {
         V *vout = (V *)a.vout[c3];
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
             if (c < nv) vout[colq(k, c)] = U[(size_t)c3 * nz * TK + idx];
         }
     }
@@ -351,6 +310,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
 // ----------------------------------------------------------------------------------------------
 template <typename T, class E>
 __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, typename E::Desc fd, FusedArgs a, int TK) {
+    const int lgTK = lg2(TK);
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nz = g.nz, nzp = g.nzp, L = fd.L;
@@ -360,7 +320,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
     const int kx0 = blockIdx.x * TK, ky = blockIdx.y;
     const int nv = min(TK, g.nxh - kx0);
     auto colq = [&](int z, int c) { return fidx<T>(g, z, ky, kx0 + c); };
-    const T dt = (T)a.dt, kap = (T)a.kappa, rmp = (T)a.rmp, inz = (T)1 / (T)nz;
+    const T dt = (T)a.dt, kap = (T)a.kappa, rmp = (T)a.rmp, inz = (T)1 / (T)nz, xtemp = (T)a.xtemp;
     // 1. NL_theta forward, heat current, filter, laplak, update.  vz is copied into Th while
     //    NL_theta is transformed; theta and cold go into the FFT buffer afterwards.
     {
@@ -377,13 +337,13 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
         async_wait();
         __syncthreads();
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
             V n = mk<T>(0, 0);
             if (c < nv) {
                 const int kx = kx0 + c;
                 n = R[E::pos(k, fd) * TK + c];
                 const V w = Th[idx];
-                n = mk<T>(n.x - (T)a.xtemp * w.x, n.y - (T)a.xtemp * w.y);
+                n = mk<T>(n.x - xtemp * w.x, n.y - xtemp * w.y);
                 n = cscale(n, g.FX<T>(kx));
                 n = cscale(n, g.FY<T>(ky));
                 n = cscale(n, g.FZ<T>(k));
@@ -397,7 +357,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
         async_wait();
         __syncthreads();
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
             if (c >= nv) { Th[idx] = mk<T>(0, 0); continue; }
             const int kx = kx0 + c;
             const T k2 = g.KX<T>(kx) * g.KX<T>(kx) + g.KY<T>(ky) * g.KY<T>(ky) + g.KZ<T>(k) * g.KZ<T>(k);
@@ -414,7 +374,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
         __syncthreads();
         V *R = E::run(X, Y, TK, fd, +1);
         for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
             Th[idx] = (k == 0 || k == nzp - 1) ? mk<T>(0, 0) : cscale(R[E::pos(k, fd) * TK + c], inz);
         }
         __syncthreads();
@@ -424,7 +384,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
         __syncthreads();
         R = E::run(X, Y, TK, fd, -1);
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
             const int kx = min(kx0 + c, g.nxh - 1);
             V v = R[E::pos(k, fd) * TK + c];
             v = cscale(v, g.FX<T>(kx));
@@ -441,7 +401,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
         V *R = E::run(X, Y, TK, fd, +1);
         V *side = (V *)a.side;
         for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
             const V v = cscale(R[E::pos(k, fd) * TK + c], inz);
             Th[idx] = v;
             const int kx = kx0 + c;
@@ -456,7 +416,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
         R = E::run(X, Y, TK, fd, -1);
         V *out = (V *)a.vout[3];
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
             const int kx = kx0 + c;
             if (c < nv && kx != 0 && kx != g.nxh - 1) out[colq(k, c)] = R[E::pos(k, fd) * TK + c];
         }
@@ -470,7 +430,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_theta_herm(Geo g, t
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nzp = g.nzp, nz = g.nz, L = fd.L;
-    const int TK = 2;
+    const int TK = 2, lgTK = 1;
     V *X = (V *)smem_raw, *Y = X + (size_t)L * TK;
     const int sel = blockIdx.y;                 // 0: kx = 0, 1: kx = nx/2
     const int kx = sel == 0 ? 0 : g.nxh - 1;
@@ -479,7 +439,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_theta_herm(Geo g, t
     const V *side = (const V *)a.side;
     const V *s1 = side + ((size_t)sel * g.ny + ky) * nzp, *s2 = side + ((size_t)sel * g.ny + kym) * nzp;
     for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
-        const int k = idx / TK, c = idx % TK;
+        const int k = idx >> lgTK, c = idx & (TK - 1);
         const V p = s1[k], m = s2[k];
         // column c = 0 holds ky, c = 1 holds -ky
         const V h = c == 0 ? mk<T>((T)0.5 * (p.x + m.x), (T)0.5 * (p.y - m.y)) : mk<T>((T)0.5 * (m.x + p.x), (T)0.5 * (m.y - p.y));
@@ -491,7 +451,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_theta_herm(Geo g, t
     V *R = E::run(X, Y, TK, fd, -1);
     V *out = (V *)a.vout[3];
     for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
-        const int k = idx / TK, c = idx % TK;
+        const int k = idx >> lgTK, c = idx & (TK - 1);
         if (c == 1 && kym == ky) continue;
         out[fidx<T>(g, k, c == 0 ? ky : kym, kx)] = R[E::pos(k, fd) * TK + c];
     }

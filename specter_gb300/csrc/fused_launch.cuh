@@ -13,10 +13,9 @@ template <typename T, class E>
 int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int which, double bytes) {
     const size_t es = sizeof(C2<T>);
     const size_t L = (size_t)fd.L;
-    const int d = P.oz;
     auto smem = [&](int tk) -> size_t {
         if (which == kFusedVelocity)
-            return (3 * (size_t)P.nz + E::kBuffers * L) * tk * es + (2 * (size_t)kThreads + (size_t)tk * (2 + 4 * d)) * 16 +
+            return (3 * (size_t)P.nz + E::kBuffers * L) * tk * es + (2 * (size_t)kThreads + (size_t)tk * 2) * 16 +
                    (size_t)tk * sizeof(LapCol<T>);
         if (which == kFusedTheta) return ((size_t)P.nz + E::kBuffers * L) * tk * es;
         return E::kBuffers * L * 2 * es;
@@ -26,7 +25,7 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
         tk = 0;
         const size_t budget = which == kFusedVelocity ? 200 * 1024 : 110 * 1024;
         for (int t : {16, 8, 4, 2, 1})
-            if (smem(t) <= budget) { tk = t; break; }
+            if (t <= P.tile_cap[Plan::kTileFused] && smem(t) <= budget) { tk = t; break; }
         if (!tk) { set_error("z length too large for the fused column kernels"); return ERR_SHAPE; }
     }
     const size_t sm = smem(tk);

@@ -92,6 +92,7 @@ struct ZInvArgs {
 
 template <typename T, class E>
 __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_inverse(Geo g, typename E::Desc fd, ZInvArgs a, int TK) {
+    const int lgTK = lg2(TK);
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * TK;
@@ -101,6 +102,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_inverse(Geo g, ty
     const int nv = min(TK, g.nxh - kx0);
     const size_t zstride = (size_t)g.ny * g.ldx;
     const V *src = in + (size_t)ky * g.ldx + kx0;
+    const T sc = (T)a.scale;
     if (a.staged) tile_load_async(S, src, zstride, g.nz, TK, nv);
     for (int pass = 1; pass >= 0; pass--) {  // derivative output first: out0 may alias in
         V *out = (V *)(pass == 0 ? a.out0[f] : a.out1[f]);
@@ -110,24 +112,24 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_inverse(Geo g, ty
             __syncthreads();
             for (int idx = threadIdx.x; idx < g.nz * TK; idx += blockDim.x) {
                 const V v = S[idx];
-                X[idx] = pass == 1 ? cimk(g.KZ<T>(idx / TK), v) : v;
+                X[idx] = pass == 1 ? cimk(g.KZ<T>(idx >> lgTK), v) : v;
             }
         } else {
             tile_load_async(X, src, zstride, g.nz, TK, nv);
             async_wait();
             if (pass == 1) {
                 __syncthreads();
-                for (int idx = threadIdx.x; idx < g.nz * TK; idx += blockDim.x) X[idx] = cimk(g.KZ<T>(idx / TK), X[idx]);
+                for (int idx = threadIdx.x; idx < g.nz * TK; idx += blockDim.x) X[idx] = cimk(g.KZ<T>(idx >> lgTK), X[idx]);
             }
         }
         __syncthreads();
         V *R = E::run(X, Y, TK, fd, +1);
         const V *add = (const V *)a.add[f];
         for (int idx = threadIdx.x; idx < a.nrows * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
             if (c >= nv) continue;
             V v = R[E::pos(k, fd) * TK + c];
-            if (k < a.scale_rows) v = cscale(v, (T)a.scale);
+            if (k < a.scale_rows) v = cscale(v, sc);
             const size_t q = fidx<T>(g, k, ky, kx0 + c);
             if (pass == 0 && add) v = cadd(v, add[q]);
             out[q] = v;
@@ -149,10 +151,11 @@ struct ZFwdArgs {
 
 template <typename T>
 __device__ __forceinline__ void fc_continuation(const Geo &g, C2<T> *X, int TK) {
+    const int lgTK = lg2(TK);
     // X holds rows [0, nzp) of TK columns; fill rows [nzp, nz)
     const int C = g.cz, d = g.oz, n = g.nz;
     for (int idx = threadIdx.x; idx < C * TK; idx += blockDim.x) {
-        const int ii = idx / TK, c = idx % TK;
+        const int ii = idx >> lgTK, c = idx & (TK - 1);
         const C2<T> t0 = X[(n - C - d) * TK + c], b0 = X[(d - 1) * TK + c];
         const double a0 = __ldg(g.dir + ii), a1 = __ldg(g.dir + (C - 1 - ii));
         double ar = a0 * (double)t0.x + a1 * (double)b0.x;
@@ -169,6 +172,7 @@ __device__ __forceinline__ void fc_continuation(const Geo &g, C2<T> *X, int TK) 
 
 template <typename T, class E>
 __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_forward(Geo g, typename E::Desc fd, ZFwdArgs a, int TK) {
+    const int lgTK = lg2(TK);
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * TK;
@@ -188,7 +192,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_forward(Geo g, ty
     __syncthreads();
     V *R = E::run(X, Y, TK, fd, -1);
     for (int idx = threadIdx.x; idx < g.nz * TK; idx += blockDim.x) {
-        const int k = idx / TK, c = idx % TK;
+        const int k = idx >> lgTK, c = idx & (TK - 1);
         if (c < nv) out[fidx<T>(g, k, ky, kx0 + c)] = R[E::pos(k, fd) * TK + c];
     }
 }
@@ -207,6 +211,7 @@ struct YArgs {
 
 template <typename T, class E>
 __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass(Geo g, typename E::Desc fd, YArgs a, int TK) {
+    const int lgTK = lg2(TK);
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * TK;
@@ -214,6 +219,8 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass(Geo g, typen
     const int kx0 = blockIdx.x * TK, z = blockIdx.y, f = blockIdx.z;
     const V *in = (const V *)a.in[f];
     const int nv = min(TK, g.nxh - kx0);
+    const T sc = (T)a.scale;
+    const bool scaled = a.scale != 1.0;
     const V *src = in + (size_t)z * g.ny * g.ldx + kx0;
     if (a.staged) tile_load_async(S, src, (size_t)g.ldx, g.ny, TK, nv);
     for (int pass = 1; pass >= 0; pass--) {  // derivative output first: out0 may alias in
@@ -224,23 +231,23 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass(Geo g, typen
             __syncthreads();
             for (int idx = threadIdx.x; idx < g.ny * TK; idx += blockDim.x) {
                 const V v = S[idx];
-                X[idx] = pass == 1 ? cimk(g.KY<T>(idx / TK), v) : v;
+                X[idx] = pass == 1 ? cimk(g.KY<T>(idx >> lgTK), v) : v;
             }
         } else {
             tile_load_async(X, src, (size_t)g.ldx, g.ny, TK, nv);
             async_wait();
             if (pass == 1) {
                 __syncthreads();
-                for (int idx = threadIdx.x; idx < g.ny * TK; idx += blockDim.x) X[idx] = cimk(g.KY<T>(idx / TK), X[idx]);
+                for (int idx = threadIdx.x; idx < g.ny * TK; idx += blockDim.x) X[idx] = cimk(g.KY<T>(idx >> lgTK), X[idx]);
             }
         }
         __syncthreads();
         V *R = E::run(X, Y, TK, fd, a.sign);
         for (int idx = threadIdx.x; idx < g.ny * TK; idx += blockDim.x) {
-            const int k = idx / TK, c = idx % TK;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
             if (c < nv) {
                 V v = R[E::pos(k, fd) * TK + c];
-                if (a.scale != 1.0) v = cscale(v, (T)a.scale);
+                if (scaled) v = cscale(v, sc);
                 out[fidx<T>(g, z, k, kx0 + c)] = v;
             }
         }
@@ -261,11 +268,12 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass(Geo g, typen
 // dx = 1 first multiplies the spectrum by i kx (the x derivative).
 template <typename T>
 __device__ __forceinline__ void c2r_pre(const Geo &g, const C2<T> *S, C2<T> *Z, int RB, int SP, int dx = 0) {
+    const int lgRB = lg2(RB);
     using V = C2<T>;
     const V *xtw = (const V *)g.xtw;
     const int H = g.H;
     for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
-        const int k = idx / RB, r = idx % RB;
+        const int k = idx >> lgRB, r = idx & (RB - 1);
         V xk = S[k * SP + r], xm = S[(H - k) * SP + r];
         if (dx) {
             xk = cimk(g.KX<T>(k), xk);
@@ -287,11 +295,12 @@ __device__ __forceinline__ void c2r_pre(const Geo &g, const C2<T> *S, C2<T> *Z, 
 template <typename T, class E, bool NAT = false>
 __device__ __forceinline__ void r2c_post(const Geo &g, const typename E::Desc &fd, const C2<T> *Z, C2<T> *S, int RB,
                                          int SP) {
+    const int lgRB = lg2(RB);
     using V = C2<T>;
     const V *xtw = (const V *)g.xtw;
     const int H = g.H;
     for (int idx = threadIdx.x; idx < (H + 1) * RB; idx += blockDim.x) {
-        const int k = idx / RB, r = idx % RB;
+        const int k = idx >> lgRB, r = idx & (RB - 1);
         const int p0 = NAT ? k % H : E::pos(k % H, fd), p1 = NAT ? (H - k) % H : E::pos((H - k) % H, fd);
         const V zk = Z[p0 * RB + r], zm = cconj(Z[p1 * RB + r]);
         const V e = cadd(zk, zm), d = csub(zk, zm);
@@ -303,9 +312,14 @@ __device__ __forceinline__ void r2c_post(const Geo &g, const typename E::Desc &f
 // shared [rows][SP] staging -> rows of a global array (row stride ld), rows < nv
 template <typename V>
 __device__ __forceinline__ void rows_store(V *out, size_t ld, const V *S, int rows, int SP, int nv) {
+    // (r, k) = divmod(idx, rows), advanced by blockDim.x without dividing per element
+    const int sr = blockDim.x / rows, sk = blockDim.x - sr * rows;
+    int r = threadIdx.x / rows, k = threadIdx.x - r * rows;
     for (int idx = threadIdx.x; idx < rows * nv; idx += blockDim.x) {
-        const int r = idx / rows, k = idx % rows;
         out[(size_t)r * ld + k] = S[k * SP + r];
+        r += sr;
+        k += sk;
+        if (k >= rows) { k -= rows; r++; }
     }
 }
 
@@ -325,6 +339,7 @@ __host__ __device__ inline size_t x_pass_elems(const typename E::Desc &fd, int n
 
 template <typename T, class E>
 __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_r2c(Geo g, typename E::Desc fd, XArgs a, int RB) {
+    const int lgRB = lg2(RB);
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int SP = RB + 1;
@@ -339,13 +354,16 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_r2c(Geo g, typena
     rows_load_async(S, (const V *)(in + (size_t)row0 * g.nx), (size_t)H, H, RB, nv, SP);
     async_wait();
     __syncthreads();
-    for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) X[idx] = S[(idx / RB) * SP + idx % RB];
+    for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) X[idx] = S[(idx >> lgRB) * SP + (idx & (RB - 1))];
     __syncthreads();
     V *R = E::run(X, Y, RB, fd, -1);
     r2c_post<T, E>(g, fd, R, S, RB, SP);
     __syncthreads();
-    if (a.scale != 1.0)
-        for (int idx = threadIdx.x; idx < g.nxh * SP; idx += blockDim.x) S[idx] = cscale(S[idx], (T)a.scale);
+    if (a.scale != 1.0) {
+        const T sc = (T)a.scale;
+    const bool scaled = a.scale != 1.0;
+        for (int idx = threadIdx.x; idx < g.nxh * SP; idx += blockDim.x) S[idx] = cscale(S[idx], sc);
+    }
     __syncthreads();
     rows_store(out + (size_t)row0 * g.ldx, (size_t)g.ldx, S, g.nxh, SP, nv);
 }
@@ -353,6 +371,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_r2c(Geo g, typena
 // x pass C2R: r[row] = IFFT_x(in[row]) (Hermitian half spectrum; Im of kx=0, nx/2 ignored)
 template <typename T, class E>
 __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_c2r(Geo g, typename E::Desc fd, XArgs a, int RB) {
+    const int lgRB = lg2(RB);
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int SP = RB + 1;
@@ -370,10 +389,11 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_c2r(Geo g, typena
     V *R = E::run(X, Y, RB, fd, +1);
     const int H = g.H;
     const T sc = (T)a.scale;
+    const bool scaled = a.scale != 1.0;
     for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
-        const int m = idx / RB, r = idx % RB;
+        const int m = idx >> lgRB, r = idx & (RB - 1);
         V v = R[E::pos(m, fd) * RB + r];
-        if (a.scale != 1.0) v = cscale(v, sc);
+        if (scaled) v = cscale(v, sc);
         S[m * SP + r] = v;
     }
     __syncthreads();
@@ -423,6 +443,7 @@ __host__ __device__ inline size_t x_nl_elems(const typename E::Desc &fd, int nxh
 // S while input t is transformed.
 template <typename T, class E>
 __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, typename E::Desc fd, XNLArgs a, int RB) {
+    const int lgRB = lg2(RB);
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int H = g.H, L = fd.L, nxh = g.nxh, SP = RB + 1;
@@ -452,7 +473,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, 
         V *R = E::run(X, Y, RB, fd, +1);
         if (term < 2) {
             for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
-                const int m = idx / RB, r = idx % RB;
+                const int m = idx >> lgRB, r = idx & (RB - 1);
                 const V p = R[E::pos(m, fd) * RB + r];
                 if (term < 0) {
                     U[(size_t)i * H * RB + idx] = p;
@@ -467,7 +488,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, 
         } else {
             // (acc + u_z d/dz v_i) * tmp in place, forward transform from permuted order, R2C
             for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
-                const int m = idx / RB, r = idx % RB;
+                const int m = idx >> lgRB, r = idx & (RB - 1);
                 const int q = E::pos(m, fd) * RB + r;
                 const V u = U[(size_t)2 * H * RB + idx], p = R[q], acc = A[idx];
                 R[q] = mk<T>((acc.x + u.x * p.x) * tmp, (acc.y + u.y * p.y) * tmp);

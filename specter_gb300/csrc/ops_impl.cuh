@@ -78,7 +78,7 @@ static int launch_z_inverse(Plan &P, const ZInvArgs &a0, int nf) {
     const size_t es = sizeof(C2<T>);
     ZInvArgs a = a0;
     a.staged = two_outputs(a.out0, a.out1, nf);
-    const int tk = pick_tile((2 * (size_t)P.tz.d.L + (a.staged ? P.nz : 0)) * es);
+    const int tk = P.capped(pick_tile((2 * (size_t)P.tz.d.L + (a.staged ? P.nz : 0)) * es), Plan::kTileZ);
     if (!tk) { set_error("z length too large for shared memory"); return ERR_SHAPE; }
     const size_t sm = (2 * (size_t)P.tz.d.L + (a.staged ? P.nz : 0)) * tk * es;
     double bytes = 0;
@@ -95,7 +95,7 @@ static int launch_z_inverse(Plan &P, const ZInvArgs &a0, int nf) {
 template <typename T>
 static int launch_z_forward(Plan &P, const ZFwdArgs &a, int nf) {
     const size_t es = sizeof(C2<T>);
-    const int tk = pick_tile(2 * (size_t)P.tz.d.L * es);
+    const int tk = P.capped(pick_tile(2 * (size_t)P.tz.d.L * es), Plan::kTileZ);
     if (!tk) { set_error("z length too large for shared memory"); return ERR_SHAPE; }
     const size_t sm = 2 * (size_t)P.tz.d.L * tk * es;
     const double bytes = nf * (cplx_rows(P, P.nzp) + cplx_rows(P, P.nz));
@@ -112,7 +112,7 @@ static int launch_y(Plan &P, const YArgs &a0, int nf, int nplanes) {
     const size_t es = sizeof(C2<T>);
     YArgs a = a0;
     a.staged = two_outputs(a.out0, a.out1, nf);
-    const int tk = pick_tile((2 * (size_t)P.ty.d.L + (a.staged ? P.ny : 0)) * es);
+    const int tk = P.capped(pick_tile((2 * (size_t)P.ty.d.L + (a.staged ? P.ny : 0)) * es), Plan::kTileY);
     if (!tk) { set_error("y length too large for shared memory"); return ERR_SHAPE; }
     const size_t sm = (2 * (size_t)P.ty.d.L + (a.staged ? P.ny : 0)) * tk * es;
     double bytes = 0;
@@ -130,7 +130,7 @@ static int launch_x(Plan &P, const XArgs &a, int nf, bool r2c) {
     const size_t es = sizeof(C2<T>);
     int rb = 0;
     for (int t : {16, 8, 4, 2, 1})
-        if (x_pass_elems<GenericFFT<T>>(P.tx.d, P.nxh, t) * es <= kSmemBudget) { rb = t; break; }
+        if (t <= P.tile_cap[Plan::kTileX] && x_pass_elems<GenericFFT<T>>(P.tx.d, P.nxh, t) * es <= kSmemBudget) { rb = t; break; }
     if (!rb) { set_error("x length too large for shared memory"); return ERR_SHAPE; }
     const size_t sm = x_pass_elems<GenericFFT<T>>(P.tx.d, P.nxh, rb) * es;
     const dim3 grid(cdiv(a.nrows * P.ny, rb), 1, nf);
@@ -155,7 +155,7 @@ static int launch_x_nl(Plan &P, const XNLArgs &a) {
     const size_t es = sizeof(C2<T>);
     int rb = 0;
     for (int t : {16, 8, 4, 2, 1})
-        if (x_nl_elems<GenericFFT<T>>(P.tx.d, P.nxh, P.H, t) * es <= kSmemBudget) { rb = t; break; }
+        if (t <= P.tile_cap[Plan::kTileX] && x_nl_elems<GenericFFT<T>>(P.tx.d, P.nxh, P.H, t) * es <= kSmemBudget) { rb = t; break; }
     if (!rb) { set_error("x length too large for shared memory"); return ERR_SHAPE; }
     const size_t sm = x_nl_elems<GenericFFT<T>>(P.tx.d, P.nxh, P.H, rb) * es;
     const int nc = a.c1 - a.c0;

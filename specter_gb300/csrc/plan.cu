@@ -252,13 +252,27 @@ int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], cons
 }
 
 void *Plan::scratch_field(int i) {
-    while ((int)scratch.size() <= i) {
+    if ((int)scratch.size() <= i) scratch.resize(i + 1, nullptr);
+    if (!scratch[i]) {
         void *m = nullptr;
-        if (cudaMalloc(&m, field_bytes()) != cudaSuccess) return nullptr;
+        if (cudaMalloc(&m, field_bytes()) != cudaSuccess) { cudaGetLastError(); return nullptr; }
         cudaMemsetAsync(m, 0, field_bytes(), stream);
-        scratch.push_back(m);
+        scratch[i] = m;
     }
     return scratch[i];
+}
+
+unsigned long long plan_bytes(const Plan &P) {
+    unsigned long long b = 0;
+    for (void *m : P.scratch) b += m ? P.field_bytes() : 0;
+    b += (P.kx.size() + P.ky.size() + P.kz.size() + P.z.size() + P.dir.size() + P.fx.size() + P.fy.size() + P.fz.size()) * 12ull;
+    auto tab = [](const FFTTable &t, size_t es) { return t.mem ? (unsigned long long)(4 * (size_t)t.d.L + 2 * (size_t)t.d.n) * es : 0ull; };
+    const size_t es = P.elt();
+    b += tab(P.tx, es) + tab(P.ty, es) + tab(P.tz, es);
+    auto tab4 = [](const FFT4Table &t) { return t.mem ? (unsigned long long)(4 * (size_t)t.d.L + (size_t)t.d.n) * 8 : 0ull; };
+    b += tab4(P.tx4) + tab4(P.ty4) + tab4(P.tz4);
+    b += (unsigned long long)(P.H + 1) * es + (unsigned long long)P.nred * 8 + (unsigned long long)P.nz * 16;
+    return b;
 }
 
 static cudaEvent_t take_event(Plan *p) {

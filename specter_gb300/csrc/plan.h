@@ -84,6 +84,11 @@ struct Plan {
     // kernel accounting: launches counted always; with profiling on, every launch is bracketed
     // by CUDA events on the plan stream and attributed to its kernel name with its
     // algorithmic bytes (compulsory reads + writes of that launch)
+    // Upper bounds on the tile width of each pass family (z passes, y passes, x passes, fused
+    // column kernels), set by the autotuner; a launcher uses min(cap, largest width that fits).
+    enum { kTileZ = 0, kTileY = 1, kTileX = 2, kTileFused = 3 };
+    int tile_cap[4] = {16, 16, 16, 16};
+    int capped(int t, int kind) const { return t < tile_cap[kind] ? t : tile_cap[kind]; }
     long long launches = 0;
     bool profile = false;
     struct Rec { const char *name; double bytes; cudaEvent_t a, b; };
@@ -106,6 +111,9 @@ struct Plan {
 int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], const double len[3],
                 const char *tdir, int prec);
 void plan_destroy(Plan *p);
+// device bytes held by the plan: tables and the scratch fields allocated so far (an estimate
+// for the tables, exact for the scratch fields)
+unsigned long long plan_bytes(const Plan &P);
 int build_fft_table(FFTTable &t, int n, Prec prec);
 void free_fft_table(FFTTable &t);
 int build_fft4_table(FFT4Table &t, int n);  // fast_f32.cu

@@ -1,0 +1,125 @@
+"""Batched ensemble of independent HD channel instances on one GPU.
+
+Each instance is its own plan and solver (uneven grids are allowed); the FP32-bulk solvers are
+autotuned per plan (tile-width caps, ``Solver.autotune``) and one RK step of all instances is
+captured as a single CUDA graph whose branches are the instances' plan streams, so that one
+graph launch advances the whole ensemble by one RK step and the instances' kernels overlap on
+the device.
+
+    python -m specter_gb300.ensemble --instances 64 --steps 200 --seq-sample 16
+
+Instance draw (seeded, numpy PCG64): nx, ny in {32, 48, 64, 96}, nz (physical) in {33, 65, 97}
+(+25 FC-Gram points), z in [0, 2], nu log-uniform in [2e-4, 2e-3], RK2, dt = 1e-4, and the
+channel initial field of specter_gb300.initial (Poiseuille + solenoidal perturbation, |k| <= 8,
+amplitude 0.05) with its own seed.  The comparison runs the same instances one after another
+through the plain FP64 form (no graph), optionally on a sample of them.  Prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import time
+
+import numpy as np
+
+GRID_XY = (32, 48, 64, 96)
+GRID_Z = (33, 65, 97)
+
+
+def draw(n, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        out.append(dict(nx=int(rng.choice(GRID_XY)), ny=int(rng.choice(GRID_XY)), nzp=int(rng.choice(GRID_Z)),
+                        nu=float(math.exp(rng.uniform(math.log(2e-4), math.log(2e-3)))), seed=int(seed) * 1000 + i,
+                        Lz=2.0, dt=1e-4, ord=2, amp=0.05, kmax=8))
+    return out
+
+
+def make(api, initial, inst, precision):
+    plan = api.Plan((inst["nx"], inst["ny"], inst["nzp"] + 25), (0, 0, 25), (0, 0, 5), (1.0, 1.0, inst["Lz"]),
+                    precision=precision)
+    s = api.Solver(plan, api.HD, ord=inst["ord"], dt=inst["dt"], nu=inst["nu"])
+    v = initial.channel_velocity(plan, seed=inst["seed"], amp=inst["amp"], kmax=inst["kmax"])
+    for f, sp in zip((s.vx, s.vy, s.vz), initial.to_spectral(plan, v)):
+        f.copy_from(sp)
+    s.pr.zero()
+    plan.synchronize()
+    return plan, s
+
+
+def rel_l2(a, b):
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a))
+
+
+def run(instances=64, steps=200, seed=20261203, seq_sample=None, autotune=True):
+    from specter_gb300 import api, initial
+    insts = draw(instances, seed)
+    t0 = time.perf_counter()
+    built = [make(api, initial, x, api.FP32) for x in insts]
+    t_build = time.perf_counter() - t0
+    caps = []
+    t0 = time.perf_counter()
+    for _, s in built:
+        caps.append(s.autotune() if autotune else None)
+    t_tune = time.perf_counter() - t0
+    solvers = [s for _, s in built]
+    graph = api.Graph(solvers, nsteps=1)
+    for p, _ in built:
+        p.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        graph.launch()
+    graph.synchronize()
+    t_run = time.perf_counter() - t0
+    for s in solvers:
+        s.check()
+    solves_per_s = instances / t_run
+    pts = sum(x["nx"] * x["ny"] * x["nzp"] * x["ord"] for x in insts) * steps
+    result = {"instances": instances, "steps": steps, "seed": seed, "precision": "fp32-bulk",
+              "graph_kernels_per_step": graph.kernels, "seconds": round(t_run, 4),
+              "solves_per_s": round(solves_per_s, 3), "mpts_stages_per_s": round(pts / t_run / 1e6, 2),
+              "build_s": round(t_build, 2), "autotune_s": round(t_tune, 2), "caps": caps}
+    # sequential plain FP64 on a sample (first k instances): time per solve, error of the ensemble
+    k = instances if seq_sample is None else min(seq_sample, instances)
+    if k > 0:
+        t_seq, errs = 0.0, []
+        for i in range(k):
+            p64, s64 = make(api, initial, insts[i], api.FP64)
+            t0 = time.perf_counter()
+            s64.step(steps)
+            p64.synchronize()
+            t_seq += time.perf_counter() - t0
+            s64.check()
+            s32 = solvers[i]
+            e = max(rel_l2(a.download().astype(np.complex128), b.download())
+                    for a, b in zip((s32.vx, s32.vy, s32.vz), (s64.vx, s64.vy, s64.vz)))
+            errs.append(e)
+            s64.close()
+            p64.close()
+        seq_solves = k / t_seq
+        result.update({"sequential_fp64": {"sample": k, "seconds": round(t_seq, 3),
+                                           "solves_per_s": round(seq_solves, 4)},
+                       "speedup_vs_sequential_fp64": round(solves_per_s / seq_solves, 2),
+                       "fp32_vs_fp64_rel_l2_max": max(errs), "fp32_vs_fp64_rel_l2_median": float(np.median(errs))})
+    graph.close()
+    return result, insts, built
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--instances", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--seq-sample", type=int, default=None, help="instances run through sequential FP64")
+    ap.add_argument("--no-autotune", action="store_true")
+    args = ap.parse_args(argv)
+    res, _, _ = run(args.instances, args.steps, args.seed, args.seq_sample, not args.no_autotune)
+    print(json.dumps(res), flush=True)
+    return res
+
+
+if __name__ == "__main__":
+    main()
