@@ -119,13 +119,19 @@ def dominant_roofline(report, hbm_peak, traffic_table):
 
 
 def load_traffic():
-    """Per-launch DRAM bytes of each kernel from the committed ncu summary (profiles/)."""
-    path = os.path.join(ROOT, "profiles", "dram_traffic_bouss512.json")
+    """Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of each kernel from
+    the committed ncu summary of this workload: the rows '| kernel | launches | bytes per launch |'
+    of profiles/dram_traffic_bouss512.md."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic_bouss512.md")
+    out = {}
     try:
-        with open(path) as f:
-            return json.load(f)
-    except Exception:
-        return {}
+        for ln in open(path):
+            cells = [c.strip() for c in ln.strip().strip("|").split("|")]
+            if len(cells) >= 3 and cells[2].replace(".", "").replace("e", "").replace("+", "").isdigit():
+                out[cells[0]] = float(cells[2])
+    except OSError:
+        pass
+    return out
 
 
 def cpu_baseline(steps, warmup, threads=None):

@@ -38,7 +38,7 @@ enum {
 
 enum { SPECTER_FP64 = 0, SPECTER_FP32 = 1 };            /* plan precision */
 enum { SPECTER_COMPLEX = 0, SPECTER_REAL = 1 };         /* field kind */
-enum { SPECTER_HD = 0, SPECTER_BOUSS = 1 };             /* solver (src/include/hd, bouss) */
+enum { SPECTER_HD = 0, SPECTER_BOUSS = 1, SPECTER_ROTBOUSS = 2 };  /* solver (src/include/hd, bouss, rotbouss) */
 
 typedef struct specter_plan specter_plan;
 typedef struct specter_field specter_field;
@@ -49,6 +49,11 @@ int specter_version(void);
 int specter_device_count(int *count);
 /* selects the CUDA device used by plans created afterwards on the calling thread */
 int specter_set_device(int device);
+/* FC-Gram table validation (no device work): reads A{C}-{d}.dat and Q{d}.dat under tdir as
+ * load_dirichlet_tables does (src/fftp/fcgram_mod.f90:180-257) and returns
+ * out = {max |Q^T Q - I|, max |dir|, max_i sum_j |dir_ij|} for dir = A Q^T: the Gram basis'
+ * orthonormality and the continuation's amplification of rounding in the wall-adjacent points. */
+int specter_table_check(const char *tdir, int C, int d, double out[3]);
 /* free and total device memory of the current device (admission by memory budget) */
 int specter_device_memory(unsigned long long *free_bytes, unsigned long long *total_bytes);
 
@@ -130,15 +135,17 @@ int specter_v_imposebc_and_project(specter_plan *plan, specter_field *vx, specte
 int specter_s_imposebc(specter_plan *plan, specter_field *th);                                       /* sboundary :67-119 */
 
 /* ---- solver: the RK loop (src/specter.fpp:1142-1161) with the stage bodies
- *      src/include/hd/hd_rkstep2.f90 and src/include/bouss/bouss_rkstep2.f90. */
+ *      src/include/hd/hd_rkstep2.f90, src/include/bouss/bouss_rkstep2.f90 and
+ *      src/include/rotbouss/rotbouss_rkstep2.f90. */
 typedef struct specter_solver_params {
-    int solver;              /* SPECTER_HD or SPECTER_BOUSS */
+    int solver;              /* SPECTER_HD, SPECTER_BOUSS or SPECTER_ROTBOUSS */
     int ord;                 /* RK order (parameter ORD) */
     double dt, nu, kappa;    /* &parameter dt, &velocity nu, &scalar kappa */
     double gama, xmom, xtemp;/* &boussinesq; xmom and xtemp are multiplied by gama (specter.fpp:490-491) */
     double v_zsta[2];        /* &velbound vxzsta, vyzsta */
     double v_zend[2];        /* &velbound vxzend, vyzend */
     int fused;               /* 1: fused GB300 stage kernels; 0: the reference call sequence */
+    double omega[3];         /* &rotation omegax, omegay, omegaz (SPECTER_ROTBOUSS) */
 } specter_solver_params;
 
 int specter_solver_create(specter_plan *plan, const specter_solver_params *p, specter_solver **out);

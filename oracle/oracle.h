@@ -91,6 +91,11 @@ void orc_fft_1d(int n, double *x, int sign);
 /* nsteps full RK steps; th == NULL selects the HD solver */
 void orc_run(const orc_grid *g, const orc_params *p, int nsteps,
              double *vx, double *vy, double *vz, double *th, double *pr);
+void orc_rotbouss_stage(const orc_grid *g, const orc_params *p, const double omega[3], int o,
+                        double *vx, double *vy, double *vz, double *th, double *pr,
+                        const double *C1, const double *C2, const double *C3, const double *C7);
+void orc_run_rot(const orc_grid *g, const orc_params *p, const double omega[3], int nsteps,
+                 double *vx, double *vy, double *vz, double *th, double *pr);
 
 #ifdef __cplusplus
 }

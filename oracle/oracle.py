@@ -236,9 +236,21 @@ class Grid:
                               *[_p(self._c(x)) for x in (C1, C2, C3, C7)], None, None, None, None)
         return vx, vy, vz, th, pr
 
-    def run(self, p, nsteps, vx, vy, vz, pr, th=None):
+    def rotbouss_stage(self, p, omega, o, vx, vy, vz, th, pr, C1, C2, C3, C7):
+        vx, vy, vz, th, pr = (self._c(x).copy() for x in (vx, vy, vz, th, pr))
+        om = (C.c_double * 3)(*omega)
+        lib().orc_rotbouss_stage(self.h, C.byref(p), om, o, _p(vx), _p(vy), _p(vz), _p(th), _p(pr),
+                                 *[_p(self._c(x)) for x in (C1, C2, C3, C7)])
+        return vx, vy, vz, th, pr
+
+    def run(self, p, nsteps, vx, vy, vz, pr, th=None, omega=None):
+        """RK loop; with omega the ROTBOUSS stage (th required)."""
         vx, vy, vz, pr = (self._c(x).copy() for x in (vx, vy, vz, pr))
         tha = self._c(th).copy() if th is not None else None
-        lib().orc_run(self.h, C.byref(p), nsteps, _p(vx), _p(vy), _p(vz),
-                      _p(tha) if tha is not None else None, _p(pr))
+        if omega is not None:
+            om = (C.c_double * 3)(*omega)
+            lib().orc_run_rot(self.h, C.byref(p), om, nsteps, _p(vx), _p(vy), _p(vz), _p(tha), _p(pr))
+        else:
+            lib().orc_run(self.h, C.byref(p), nsteps, _p(vx), _p(vy), _p(vz),
+                          _p(tha) if tha is not None else None, _p(pr))
         return (vx, vy, vz, pr) if th is None else (vx, vy, vz, tha, pr)

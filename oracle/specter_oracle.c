@@ -829,6 +829,54 @@ void orc_bouss_stage(const orc_grid *g, const orc_params *p, int o,
     free(C4); free(C5); free(C6); free(C8); free(R1);
 }
 
+/* ROTBOUSS stage, src/include/rotbouss/rotbouss_rkstep2.f90:1-56: the BOUSS stage with the
+ * Coriolis term 2 Om x v added to the nonlinear term (:13-17) and without the final theta
+ * filter and c2r/r2c round trip. */
+void orc_rotbouss_stage(const orc_grid *g, const orc_params *p, const double omega[3], int o,
+                        double *vx, double *vy, double *vz, double *th, double *pr,
+                        const double *C1, const double *C2, const double *C3, const double *C7) {
+    const size_t ns = NS(g);
+    const double rmp = 1 / (double)o;
+    const double ox = omega[0], oy = omega[1], oz = omega[2];
+    double *C4 = malloc(sizeof(cplx) * ns), *C5 = malloc(sizeof(cplx) * ns), *C6 = malloc(sizeof(cplx) * ns);
+    double *C8 = malloc(sizeof(cplx) * ns);
+    orc_gradre(g, vx, vy, vz, C4, C5, C6);
+    orc_advect(g, vx, vy, vz, th, C8);
+    {
+        cplx *c4 = (cplx *)C4, *c5 = (cplx *)C5, *c6 = (cplx *)C6, *c8 = (cplx *)C8;
+        const cplx *t = (const cplx *)th, *u = (const cplx *)vx, *v = (const cplx *)vy, *w = (const cplx *)vz;
+#pragma omp parallel for schedule(static)
+        for (size_t q = 0; q < ns; q++) {
+            c4[q] = c4[q] + 2 * (oy * w[q] - oz * v[q]);
+            c5[q] = c5[q] + 2 * (oz * u[q] - ox * w[q]);
+            c6[q] = c6[q] + 2 * (ox * v[q] - oy * u[q]) - p->xmom * t[q];
+            c8[q] = c8[q] - p->xtemp * w[q];
+        }
+    }
+    orc_fc_filter(g, C4); orc_fc_filter(g, C5); orc_fc_filter(g, C6); orc_fc_filter(g, C8);
+    orc_laplak(g, vx, vx); orc_laplak(g, vy, vy); orc_laplak(g, vz, vz); orc_laplak(g, th, th);
+    rk_update(g, (cplx *)vx, (const cplx *)C1, (const cplx *)C4, NULL, p->dt, p->nu, rmp);
+    rk_update(g, (cplx *)vy, (const cplx *)C2, (const cplx *)C5, NULL, p->dt, p->nu, rmp);
+    rk_update(g, (cplx *)vz, (const cplx *)C3, (const cplx *)C6, NULL, p->dt, p->nu, rmp);
+    rk_update(g, (cplx *)th, (const cplx *)C7, (const cplx *)C8, NULL, p->dt, p->kappa, rmp);
+    const double zs[2] = {p->vxzsta, p->vyzsta}, ze[2] = {p->vxzend, p->vyzend};
+    orc_v_imposebc_and_project(g, vx, vy, vz, pr, o, p->ord, zs, ze);
+    orc_s_imposebc(g, th);
+    free(C4); free(C5); free(C6); free(C8);
+}
+
+/* RK loop of the ROTBOUSS solver (rkstep1 of rotbouss_rkstep1.f90 is the BOUSS one) */
+void orc_run_rot(const orc_grid *g, const orc_params *p, const double omega[3], int nsteps,
+                 double *vx, double *vy, double *vz, double *th, double *pr) {
+    const size_t bytes = sizeof(cplx) * NS(g);
+    double *C1 = malloc(bytes), *C2 = malloc(bytes), *C3 = malloc(bytes), *C7 = malloc(bytes);
+    for (int t = 0; t < nsteps; t++) {
+        memcpy(C1, vx, bytes); memcpy(C2, vy, bytes); memcpy(C3, vz, bytes); memcpy(C7, th, bytes);
+        for (int o = p->ord; o >= 1; o--) orc_rotbouss_stage(g, p, omega, o, vx, vy, vz, th, pr, C1, C2, C3, C7);
+    }
+    free(C1); free(C2); free(C3); free(C7);
+}
+
 /* RK loop, src/specter.fpp:1142-1161: rkstep1 copies, then o = ord..1 */
 void orc_run(const orc_grid *g, const orc_params *p, int nsteps,
              double *vx, double *vy, double *vz, double *th, double *pr) {

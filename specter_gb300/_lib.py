@@ -34,6 +34,7 @@ EXPORTS = [
     "specter_solver_autotune", "specter_plan_tile_caps",
     "specter_graph_create", "specter_graph_launch", "specter_graph_synchronize", "specter_graph_kernels",
     "specter_graph_destroy", "specter_graph_query", "specter_solver_memory", "specter_device_memory",
+    "specter_table_check",
     "specter_timers", "specter_timers_reset",
     "specter_profile", "specter_profile_report", "specter_launch_count",
 ]
@@ -49,7 +50,8 @@ class SolverParams(C.Structure):
     _fields_ = [("solver", C.c_int), ("ord", C.c_int),
                 ("dt", C.c_double), ("nu", C.c_double), ("kappa", C.c_double),
                 ("gama", C.c_double), ("xmom", C.c_double), ("xtemp", C.c_double),
-                ("v_zsta", C.c_double * 2), ("v_zend", C.c_double * 2), ("fused", C.c_int)]
+                ("v_zsta", C.c_double * 2), ("v_zend", C.c_double * 2), ("fused", C.c_int),
+                ("omega", C.c_double * 3)]
 
 
 _lib = None
@@ -96,6 +98,7 @@ def load(path: str | None = None):
     L.specter_graph_query.argtypes = [VP, C.POINTER(C.c_int)]
     L.specter_solver_memory.argtypes = [VP, C.POINTER(C.c_ulonglong)]
     L.specter_device_memory.argtypes = [C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]
+    L.specter_table_check.argtypes = [C.c_char_p, C.c_int, C.c_int, PD]
     L.specter_field_create.argtypes = [VP, C.c_int, C.POINTER(VP)]
     L.specter_field_upload.argtypes = [VP, VP]
     L.specter_field_download.argtypes = [VP, VP]

@@ -19,7 +19,7 @@ from ._lib import SolverParams, SpecterError, check, load
 TABLES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tables")
 FP64, FP32 = 0, 1
 COMPLEX, REAL = 0, 1
-HD, BOUSS = 0, 1
+HD, BOUSS, ROTBOUSS = 0, 1, 2
 
 
 def _pd(a):
@@ -307,11 +307,11 @@ def s_imposebc(plan, th):
 class Solver:
     """The RK loop of src/specter.fpp:1142-1161 with the HD or BOUSS stage body.
 
-    fused=True runs the GB300 fused stage kernels; fused=False runs the reference's call
-    sequence (gradre, fc_filter, laplak, update, v_imposebc_and_project, ...) on the GPU."""
+    solver HD, BOUSS or ROTBOUSS (rotation rate omega).  fused=True runs the GB300 fused stage
+    kernels; fused=False runs the reference's call sequence (gradre, fc_filter, laplak, update, v_imposebc_and_project, ...) on the GPU."""
 
     def __init__(self, plan: Plan, solver=HD, ord=2, dt=1e-4, nu=1e-3, kappa=0.0, gama=1.0,
-                 xmom=1.0, xtemp=1.0, v_zsta=(0.0, 0.0), v_zend=(0.0, 0.0), fused=True):
+                 xmom=1.0, xtemp=1.0, v_zsta=(0.0, 0.0), v_zend=(0.0, 0.0), fused=True, omega=(0.0, 0.0, 0.0)):
         self.plan = plan
         p = SolverParams()
         p.solver, p.ord, p.dt, p.nu, p.kappa = solver, ord, dt, nu, kappa
@@ -319,6 +319,7 @@ class Solver:
         p.v_zsta[0], p.v_zsta[1] = v_zsta
         p.v_zend[0], p.v_zend[1] = v_zend
         p.fused = 1 if fused else 0
+        p.omega[0], p.omega[1], p.omega[2] = omega
         self.params = p
         h = C.c_void_p()
         check(_L(plan).specter_solver_create(plan.h, C.byref(p), C.byref(h)))
@@ -360,6 +361,14 @@ class Solver:
         caps = (C.c_int * 4)()
         check(_L(self.plan).specter_solver_autotune(self.h, caps))
         return tuple(caps)
+
+
+def table_check(C_=25, d=5, tdir=None):
+    """Validates FC-Gram tables A{C}-{d}.dat / Q{d}.dat (default: the packaged ones): returns
+    (max |Q^T Q - I|, max |dir|, max row sum of |dir|)."""
+    out = (C.c_double * 3)()
+    check(load().specter_table_check((tdir or TABLES).encode(), int(C_), int(d), out))
+    return tuple(out)
 
 
 def device_memory():

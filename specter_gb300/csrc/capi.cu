@@ -84,6 +84,11 @@ int specter_device_count(int *count) {
     return SPECTER_OK;
 }
 
+int specter_table_check(const char *tdir, int C, int d, double out[3]) {
+    if (!out) { set_error("null argument"); return SPECTER_ERR_ARG; }
+    return table_check(tdir, C, d, out);
+}
+
 int specter_device_memory(unsigned long long *free_bytes, unsigned long long *total_bytes) {
     if (!free_bytes || !total_bytes) { set_error("null argument"); return SPECTER_ERR_ARG; }
     size_t f = 0, t = 0;
@@ -413,7 +418,10 @@ int specter_s_imposebc(specter_plan *plan, specter_field *th) {
 int specter_solver_create(specter_plan *plan, const specter_solver_params *p, specter_solver **out) {
     CHECK_PLAN(plan);
     if (!p || !out) { set_error("null argument"); return SPECTER_ERR_ARG; }
-    if ((p->solver != SPECTER_HD && p->solver != SPECTER_BOUSS) || p->ord < 1) { set_error("bad solver parameters"); return SPECTER_ERR_ARG; }
+    if ((p->solver != SPECTER_HD && p->solver != SPECTER_BOUSS && p->solver != SPECTER_ROTBOUSS) || p->ord < 1) {
+        set_error("bad solver parameters");
+        return SPECTER_ERR_ARG;
+    }
     specter_solver *s = new specter_solver();  // value-initialised: all handles null
     s->plan = plan;
     plan->refs++;
@@ -423,8 +431,9 @@ int specter_solver_create(specter_plan *plan, const specter_solver_params *p, sp
     s->sp.xmom = p->xmom * p->gama; s->sp.xtemp = p->xtemp * p->gama;
     s->sp.vzsta[0] = p->v_zsta[0]; s->sp.vzsta[1] = p->v_zsta[1];
     s->sp.vzend[0] = p->v_zend[0]; s->sp.vzend[1] = p->v_zend[1];
+    for (int i = 0; i < 3; i++) s->sp.omega[i] = p->solver == SPECTER_ROTBOUSS ? p->omega[i] : 0.0;
     s->fused = p->fused;
-    const int nc = p->solver == SPECTER_BOUSS ? 4 : 3;
+    const int nc = p->solver == SPECTER_HD ? 3 : 4;
     int st = SPECTER_OK;
     for (int i = 0; i < 4 && !st; i++) {
         s->v[i] = nullptr;
@@ -490,7 +499,7 @@ int specter_solver_stage(specter_solver *s, int o) {
 int specter_solver_step(specter_solver *s, int nsteps) {
     if (!s) { set_error("null solver"); return SPECTER_ERR_ARG; }
     Plan &P = *s->plan->p;
-    const int nc = s->sp.solver == SPECTER_BOUSS ? 4 : 3;
+    const int nc = s->sp.solver == SPECTER_HD ? 3 : 4;
     if (s->fused) {
         void *v[4] = {s->v[0]->d, s->v[1]->d, s->v[2]->d, s->v[3] ? s->v[3]->d : nullptr};
         for (int t = 0; t < nsteps; t++) {
@@ -516,7 +525,7 @@ int specter_solver_step(specter_solver *s, int nsteps) {
 int specter_solver_check(specter_solver *s) {
     if (!s) { set_error("null solver"); return SPECTER_ERR_ARG; }
     Plan &P = *s->plan->p;
-    const int nc = s->sp.solver == SPECTER_BOUSS ? 4 : 3;
+    const int nc = s->sp.solver == SPECTER_HD ? 3 : 4;
     for (int i = 0; i < nc; i++) {
         double e = 0.0;
         int st = P.prec == FP64 ? Ops<double>::variance(P, s->v[i]->d, 1, &e) : Ops<float>::variance(P, s->v[i]->d, 1, &e);
@@ -733,7 +742,7 @@ int specter_graph_query(specter_graph *g, int *done) {
 int specter_solver_memory(specter_solver *s, unsigned long long *bytes) {
     if (!s || !bytes) { set_error("null argument"); return SPECTER_ERR_ARG; }
     const Plan &P = *s->plan->p;
-    const int nc = s->sp.solver == SPECTER_BOUSS ? 4 : 3;
+    const int nc = s->sp.solver == SPECTER_HD ? 3 : 4;
     unsigned long long b = 0;
     b += (unsigned long long)(2 * nc + 1) * P.field_bytes();  // state, pr, RK start
     b += fused_bytes(P, s->fs);

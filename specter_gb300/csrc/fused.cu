@@ -100,13 +100,13 @@ int fused_create(Plan &P, const StageParams &sp, FusedState **out) {
     *out = nullptr;
     FusedState *fs = new FusedState();
     fs->sp = sp;
-    fs->nc = sp.solver == 1 ? 4 : 3;
+    fs->nc = sp.solver >= 1 ? 4 : 3;
     bool ok = true;
     for (int i = 0; i < fs->nc; i++) {
         ok = ok && cudaMalloc(&fs->X1[i], P.field_bytes()) == cudaSuccess;
         if (sp.ord >= 3) ok = ok && cudaMalloc(&fs->X2[i], P.field_bytes()) == cudaSuccess;
     }
-    if (sp.solver == 1) ok = ok && cudaMalloc(&fs->side, 2 * (size_t)P.ny * P.nzp * P.elt()) == cudaSuccess;
+    if (sp.solver == 1) ok = ok && cudaMalloc(&fs->side, 2 * (size_t)P.ny * P.nzp * P.elt()) == cudaSuccess;  // BOUSS only
     for (int i = 0; i < 2; i++) ok = ok && cudaMalloc(&fs->E[i], P.field_bytes()) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
@@ -155,7 +155,7 @@ template <typename T>
 static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], const void *const cold[4],
                      void *const vout[4], void *pr) {
     const StageParams &sp = fs->sp;
-    const bool bouss = sp.solver == 1;
+    const bool bouss = sp.solver >= 1, rot = sp.solver == 2;
     const void *nl[4] = {nullptr, nullptr, nullptr, nullptr};
     const void *v3[3] = {vin[0], vin[1], vin[2]};
     int st = Ops<T>::nonlinear(P, v3, bouss ? vin[3] : nullptr, nullptr, 0, bouss ? 4 : 3, nl);
@@ -178,6 +178,8 @@ static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], c
     a.wall_tmp = tmp;
     a.vb[0] = sp.vzsta[0]; a.vb[1] = sp.vzsta[1]; a.vb[2] = sp.vzend[0]; a.vb[3] = sp.vzend[1];
     a.bouss = bouss ? 1 : 0;
+    a.rot = rot ? 1 : 0;
+    for (int i = 0; i < 3; i++) a.omega[i] = sp.omega[i];
     const double row = (double)P.ny * P.nxh * P.elt();
     // reads: NL (physical rows), vin, cold (+ theta for buoyancy), the two unit-profile
     // spectra; writes: vout and pr rows
@@ -186,7 +188,7 @@ static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], c
     if (bouss) {
         const double bt = row * (1.0 * P.nzp + 3.0 * P.nz + 1.0 * P.nz);
         if ((st = launch<T>(P, a, kFusedTheta, bt))) return st;
-        if ((st = launch<T>(P, a, kFusedHerm, 4.0 * P.ny * P.nz * P.elt()))) return st;
+        if (!rot && (st = launch<T>(P, a, kFusedHerm, 4.0 * P.ny * P.nz * P.elt()))) return st;
     }
     return OK;
 }

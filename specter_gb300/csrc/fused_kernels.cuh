@@ -34,7 +34,9 @@ struct FusedArgs {
     double dt, nu, kappa, rmp, xmom, xtemp;
     double wall_tmp;      // 1/o, or (o+1)/o when o != ord (noslip_z)
     double vb[4];         // vxzsta, vyzsta, vxzend, vyzend
+    double omega[3];      // rotation rate (rot != 0)
     int bouss;
+    int rot;              // ROTBOUSS: Coriolis term, no final theta filter / round trip
 };
 
 // Per-column laplace_z parameters in the kernel's precision: kh = |(kx, ky)| and the
@@ -131,13 +133,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
             async_wait();
             __syncthreads();
         }
-        // (a) filtered nonlinear term (minus buoyancy) -> U[c]
+        // (a) filtered nonlinear term (+ 2 Om x v, minus buoyancy) -> U[c]
+        const V *va = (const V *)a.vin[(c3 + 1) % 3], *vb = (const V *)a.vin[(c3 + 2) % 3];
+        const T oa = (T)a.omega[(c3 + 1) % 3], ob = (T)a.omega[(c3 + 2) % 3];
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
             const int k = idx >> lgTK, c = idx & (TK - 1);
             V n = mk<T>(0, 0);
             if (c < nv) {
                 const int kx = kx0 + c;
                 n = R[E::pos(k, fd) * TK + c];
+                if (a.rot) {
+                    // component c of 2 Om x v = 2 (Om_a v_b - Om_b v_a), (c, a, b) cyclic
+                    const size_t q = colq(k, c);
+                    const V pa = va[q], pb = vb[q];
+                    n = mk<T>(n.x + (T)2 * (oa * pb.x - ob * pa.x), n.y + (T)2 * (oa * pb.y - ob * pa.y));
+                }
                 if (buoy) { const V t = Uc[idx]; n = mk<T>(n.x - xmom * t.x, n.y - xmom * t.y); }
                 n = cscale(n, g.FX<T>(kx));
                 n = cscale(n, g.FY<T>(ky));
@@ -383,6 +393,14 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
         fc_continuation<T>(g, X, TK);
         __syncthreads();
         R = E::run(X, Y, TK, fd, -1);
+        if (a.rot) {  // ROTBOUSS ends the scalar update with s_imposebc (rotbouss_rkstep2.f90:56)
+            V *out = (V *)a.vout[3];
+            for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+                const int k = idx >> lgTK, c = idx & (TK - 1);
+                if (c < nv) out[colq(k, c)] = R[E::pos(k, fd) * TK + c];
+            }
+            return;
+        }
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
             const int k = idx >> lgTK, c = idx & (TK - 1);
             const int kx = min(kx0 + c, g.nxh - 1);

@@ -21,6 +21,20 @@ namespace sg {
     }                \
     }
 
+// Coriolis term of the ROTBOUSS nonlinear term, src/include/rotbouss/rotbouss_rkstep2.f90:13-17:
+// N += 2 Om x v, each component as the reference writes it.
+template <typename T>
+__global__ void k_coriolis(Geo g, C2<T> *n0, C2<T> *n1, C2<T> *n2, const C2<T> *vx, const C2<T> *vy,
+                           const C2<T> *vz, T ox, T oy, T oz) {
+    SG_ELEMS_BEGIN(g, 0, g.nz)
+    const C2<T> u = vx[q], v = vy[q], w = vz[q];
+    const T two = (T)2;
+    n0[q] = mk<T>(n0[q].x + two * (oy * w.x - oz * v.x), n0[q].y + two * (oy * w.y - oz * v.y));
+    n1[q] = mk<T>(n1[q].x + two * (oz * u.x - ox * w.x), n1[q].y + two * (oz * u.y - ox * w.y));
+    n2[q] = mk<T>(n2[q].x + two * (ox * v.x - oy * u.x), n2[q].y + two * (ox * v.y - oy * u.y));
+    SG_ELEMS_END
+}
+
 template <typename T>
 __device__ __forceinline__ T kk2_at(const Geo &g, int z, int ky, int kx) {
     const T a = g.KX<T>(kx), b = g.KY<T>(ky), c = g.KZ<T>(z);

@@ -7,13 +7,16 @@
 namespace sg {
 
 struct StageParams {
-    int solver;  // 0 HD, 1 BOUSS
+    int solver;  // 0 HD, 1 BOUSS, 2 ROTBOUSS
     int ord;
     double dt, nu, kappa, xmom, xtemp;  // xmom, xtemp already multiplied by gama
     double vzsta[2], vzend[2];
+    double omega[3];  // rotation rate (ROTBOUSS)
 };
 
 template <typename T> struct Ops {
+    // NL += 2 Om x v, component-wise as rotbouss_rkstep2.f90:13-17
+    static int coriolis(Plan &P, void *const N[3], const void *const v[3], const double omega[3]);
     // fftp
     static int fftp1d_r2c_z(Plan &P, void *inout);
     static int fftp1d_c2r_z(Plan &P, void *inout);

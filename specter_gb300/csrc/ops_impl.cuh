@@ -617,6 +617,15 @@ template <typename T> int Ops<T>::scale_real(Plan &P, void *r, double s) {
 // One RK stage: hd_rkstep2.f90:1-36 (solver 0) or bouss_rkstep2.f90:1-59 (solver 1), executed
 // as the reference's call sequence.  v = {vx, vy, vz, th}; Cold = {C1, C2, C3, C7}.
 template <typename T>
+int Ops<T>::coriolis(Plan &P, void *const N[3], const void *const v[3], const double omega[3]) {
+    Launch L(P, "coriolis", 9.0 * cplx_rows(P, P.nz));
+    k_coriolis<T><<<elem_blocks(P, P.nz), kThreads, 0, P.stream>>>(
+        P.geo, (C2<T> *)N[0], (C2<T> *)N[1], (C2<T> *)N[2], (const C2<T> *)v[0], (const C2<T> *)v[1],
+        (const C2<T> *)v[2], (T)omega[0], (T)omega[1], (T)omega[2]);
+    return check_launch("coriolis");
+}
+
+template <typename T>
 int Ops<T>::stage(Plan &P, const StageParams &sp, int o, void *const v[4], void *pr, const void *const Cold[4]) {
     void *N[4];
     for (int i = 0; i < 4; i++) {
@@ -624,9 +633,10 @@ int Ops<T>::stage(Plan &P, const StageParams &sp, int o, void *const v[4], void 
         if (!N[i]) { set_error("out of device memory"); return ERR_OOM; }
     }
     const double rmp = 1 / (double)o;
-    const bool bouss = sp.solver == 1;
+    const bool bouss = sp.solver >= 1, rot = sp.solver == 2;
     const void *vv[3] = {v[0], v[1], v[2]};
     SG_TRY(nonlinear(P, vv, bouss ? v[3] : nullptr, N, 0, bouss ? 4 : 3));
+    if (rot) SG_TRY(coriolis(P, N, vv, sp.omega));  // rotbouss_rkstep2.f90:13-17
     if (bouss) {
         SG_TRY(axpy_sub(P, N[2], v[3], sp.xmom));   // buoyancy
         SG_TRY(axpy_sub(P, N[3], v[2], sp.xtemp));  // heat current
@@ -635,6 +645,7 @@ int Ops<T>::stage(Plan &P, const StageParams &sp, int o, void *const v[4], void 
     for (int i = 0; i < 3; i++) SG_TRY(rk_update(P, v[i], Cold[i], N[i], sp.dt, sp.nu, rmp));
     if (bouss) SG_TRY(rk_update(P, v[3], Cold[3], N[3], sp.dt, sp.kappa, rmp));
     SG_TRY(v_imposebc_and_project(P, v[0], v[1], v[2], pr, o, sp.ord, sp.vzsta, sp.vzend));
+    if (rot) return s_imposebc(P, v[3]);  // no theta filter / round trip in rotbouss_rkstep2.f90
     if (bouss) {
         SG_TRY(s_imposebc(P, v[3]));
         SG_TRY(fc_filter(P, v[3]));

@@ -114,11 +114,11 @@ void free_fft_table(FFTTable &t) {
     t.mem = nullptr;
 }
 
-static int load_tables(Plan *p, const char *tdir) {
-    // load_dirichlet_tables, src/fftp/fcgram_mod.f90:180-257: raw float64 streams in Fortran
-    // order, A(C,d) and Q(d,d); dir = A * transpose(Q).
-    const int C = p->cz, d = p->oz;
-    std::vector<double> A((size_t)C * d), Q((size_t)d * d);
+// load_dirichlet_tables, src/fftp/fcgram_mod.f90:180-257: raw float64 streams in Fortran
+// order, A(C,d) and Q(d,d); dir = A * transpose(Q).
+static int read_tables(const char *tdir, int C, int d, std::vector<double> &A, std::vector<double> &Q) {
+    A.assign((size_t)C * d, 0.0);
+    Q.assign((size_t)d * d, 0.0);
     char path[4096];
     snprintf(path, sizeof path, "%s/A%d-%d.dat", tdir, C, d);
     FILE *f = fopen(path, "rb");
@@ -136,13 +136,54 @@ static int load_tables(Plan *p, const char *tdir) {
         return ERR_TABLE;
     }
     fclose(f);
-    p->dir.assign((size_t)C * d, 0.0);
+    return OK;
+}
+
+static std::vector<double> dir_from(const std::vector<double> &A, const std::vector<double> &Q, int C, int d) {
+    std::vector<double> dir((size_t)C * d, 0.0);
     for (int i = 0; i < C; i++)
         for (int j = 0; j < d; j++) {
             double s = 0.0;
             for (int l = 0; l < d; l++) s += A[i + (size_t)C * l] * Q[j + (size_t)d * l];
-            p->dir[i + (size_t)C * j] = s;
+            dir[i + (size_t)C * j] = s;
         }
+    return dir;
+}
+
+static int load_tables(Plan *p, const char *tdir) {
+    std::vector<double> A, Q;
+    const int st = read_tables(tdir, p->cz, p->oz, A, Q);
+    if (st) return st;
+    p->dir = dir_from(A, Q, p->cz, p->oz);
+    return OK;
+}
+
+int table_check(const char *tdir, int C, int d, double out[3]) {
+    if (C < 1 || d < 1 || C > 4096 || d > 64) { set_error("bad table sizes"); return ERR_ARG; }
+    std::vector<double> A, Q;
+    const int st = read_tables(tdir ? tdir : ".", C, d, A, Q);
+    if (st) return st;
+    // orthonormality of the Gram basis: max |Q^T Q - I|
+    double e = 0.0;
+    for (int i = 0; i < d; i++)
+        for (int j = 0; j < d; j++) {
+            double s = 0.0;
+            for (int l = 0; l < d; l++) s += Q[l + (size_t)d * i] * Q[l + (size_t)d * j];
+            e = std::max(e, std::fabs(s - (i == j ? 1.0 : 0.0)));
+        }
+    const std::vector<double> dir = dir_from(A, Q, C, d);
+    double mx = 0.0, rs = 0.0;
+    for (int i = 0; i < C; i++) {
+        double r = 0.0;
+        for (int j = 0; j < d; j++) {
+            mx = std::max(mx, std::fabs(dir[i + (size_t)C * j]));
+            r += std::fabs(dir[i + (size_t)C * j]);
+        }
+        rs = std::max(rs, r);
+    }
+    out[0] = e;
+    out[1] = mx;
+    out[2] = rs;
     return OK;
 }
 

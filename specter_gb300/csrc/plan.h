@@ -114,6 +114,9 @@ void plan_destroy(Plan *p);
 // device bytes held by the plan: tables and the scratch fields allocated so far (an estimate
 // for the tables, exact for the scratch fields)
 unsigned long long plan_bytes(const Plan &P);
+// FC-Gram tables A{C}-{d}.dat, Q{d}.dat under tdir: out = {max |Q^T Q - I|, max |dir|,
+// max_i sum_j |dir_ij|} with dir = A Q^T
+int table_check(const char *tdir, int C, int d, double out[3]);
 int build_fft_table(FFTTable &t, int n, Prec prec);
 void free_fft_table(FFTTable &t);
 int build_fft4_table(FFT4Table &t, int n);  // fast_f32.cu

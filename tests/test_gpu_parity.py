@@ -172,7 +172,10 @@ def test_imposebc(pair, rki):
     assert rel(ft.download(), g.s_imposebc(v[3])) < 1e-11
 
 
-@pytest.mark.parametrize("solver", [0, 1], ids=["HD", "BOUSS"])
+OMEGA = (0.3, -0.7, 2.0)
+
+
+@pytest.mark.parametrize("solver", [0, 1, 2], ids=["HD", "BOUSS", "ROTBOUSS"])
 @pytest.mark.parametrize("fused", [False, True], ids=["refseq", "fused"])
 def test_rk_step(pair, solver, fused):
     from specter_gb300 import api
@@ -182,16 +185,16 @@ def test_rk_step(pair, solver, fused):
     th = smooth_spectral(g, rng, amp=0.3)
     pr = g.fftp1d_complex_to_real_z(smooth_spectral(g, rng, amp=1e-3)) / g.nz
     kw = dict(dt=1e-3, nu=1e-2, ord=2, kappa=5e-3)
-    s = api.Solver(plan, solver, fused=fused, **kw)
+    s = api.Solver(plan, solver, fused=fused, omega=OMEGA if solver == 2 else (0.0, 0.0, 0.0), **kw)
     for fld, a in zip((s.vx, s.vy, s.vz), v):
         fld.upload(a)
     s.pr.upload(pr)
-    if solver == 1:
+    if solver >= 1:
         s.th.upload(th)
     s.step(2)
     p = g.params(**kw)
-    ref = g.run(p, 2, *v, pr, th=th if solver == 1 else None)
-    got = [f.download() for f in (s.vx, s.vy, s.vz)] + ([s.th.download()] if solver == 1 else [])
+    ref = g.run(p, 2, *v, pr, th=th if solver >= 1 else None, omega=OMEGA if solver == 2 else None)
+    got = [f.download() for f in (s.vx, s.vy, s.vz)] + ([s.th.download()] if solver >= 1 else [])
     for a, b in zip(got, ref[: len(got)]):
         assert rel(a, b) < 1e-11
     nzp = g.nz - g.cz
