@@ -193,6 +193,7 @@ def main():
     ap.add_argument("--refseq", action="store_true", help="time the reference call sequence instead of the fused stages")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--grid", default=None, help="NX,NY,NZP: another grid of the same case (profiling, sweeps)")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default tile widths")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -214,6 +215,8 @@ def main():
     if args.grid:
         cfg["nx"], cfg["ny"], cfg["nzp"] = (int(v) for v in args.grid.split(","))
     plan, s = build_solver(api, initial, cfg, api.FP32, fused=not args.refseq)
+    # tile widths of each kernel family picked by timing RK steps (state restored afterwards)
+    caps = s.autotune() if not args.no_autotune else None
     stream = torch.cuda.ExternalStream(plan.stream, device=torch.device("cuda", local))
     for _ in range(W):
         s.step(1)
@@ -282,6 +285,7 @@ def main():
                 "config": {"workload": f"BOUSS Rayleigh-Benard {cfg['nx']}x{cfg['ny']}x{cfg['nzp']} (+{cfg['cz']} FC-Gram, "
                                        f"NZ={cfg['nzp'] + cfg['cz']}), FP32-bulk, RK2, dt=1e-5",
                            "path": "reference-sequence" if args.refseq else "fused",
+                           "tile_caps_zyx_fused": list(caps) if caps else None,
                            "l2": f"inputs larger than L2 ({field_mb:.0f} MB per field), no flush",
                            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
                 "roofline": roof,

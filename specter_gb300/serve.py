@@ -11,9 +11,12 @@ The server keeps the state of every admitted simulation resident in HBM and admi
 requests in arrival order while the device memory they need fits the budget.  Each admitted
 simulation runs on its own plan stream from a captured one-step CUDA graph, launched in chunks of
 steps whenever its previous chunk has finished, so the kernels of different simulations overlap
-on the device and new requests start while others are running (continuous batching).  A
-simulation's memory is released as soon as its result is out.  Time-to-result of a request is
-its completion time minus its arrival time.
+on the device and new requests start while others are running (continuous batching).  Among the
+admitted simulations, chunks go to those with the least remaining work (grid points x stages
+left) until the running set holds `fill_points` grid points, so short requests are not held
+behind long ones (policy "srpt"; policy "all" runs every admitted simulation).  A simulation's
+memory is released as soon as its result is out.  Time-to-result of a request is its completion
+time minus its arrival time.
 
     python -m specter_gb300.serve --requests 32 --rate 50 --budget-gb 120
 
@@ -93,7 +96,8 @@ def field_bytes(req, precision):
 class Server:
     """Continuous-batching request loop (see the module docstring)."""
 
-    def __init__(self, budget_bytes, chunk=25, precision=1, keep_results=False, autotune=False):
+    def __init__(self, budget_bytes, chunk=25, precision=1, keep_results=False, autotune=False, policy="srpt",
+                 fill_points=16_000_000):
         from specter_gb300 import api, initial
         self.api, self.initial = api, initial
         self.budget = int(budget_bytes)
@@ -101,6 +105,8 @@ class Server:
         self.precision = precision
         self.keep = keep_results
         self.autotune = autotune
+        self.policy = policy
+        self.fill_points = fill_points
         self.per_field = {}  # solver kind -> device bytes per field-sized unit, measured
 
     def _estimate(self, req):
@@ -115,7 +121,18 @@ class Server:
         self.per_field[req.kind] = max(self.per_field.get(req.kind, 0.0), used / field_bytes(req, self.precision))
         req.admitted = now
         return {"req": req, "plan": plan, "solver": s, "graph": g, "remaining": req.steps, "inflight": 0,
-                "bytes": used}
+                "bytes": used, "points": req.nx * req.ny * req.nzp}
+
+    def _running_set(self, active):
+        if self.policy == "all":
+            return active
+        chosen, pts = [], 0
+        for e in sorted(active, key=lambda e: e["remaining"] * e["points"]):
+            if chosen and pts + e["points"] > self.fill_points:
+                break
+            chosen.append(e)
+            pts += e["points"]
+        return chosen
 
     def _launch(self, e):
         k = min(self.chunk, e["remaining"])
@@ -126,7 +143,7 @@ class Server:
     def run(self, requests):
         pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
         waiting, active = collections.deque(), []
-        used, peak_used, peak_active = 0, 0, 0
+        used, peak_used, peak_active, peak_running = 0, 0, 0, 0
         t0 = time.perf_counter()
         while pending or waiting or active:
             now = time.perf_counter() - t0
@@ -136,7 +153,6 @@ class Server:
                 e = self._start(waiting.popleft(), time.perf_counter() - t0)
                 used += e["bytes"]
                 active.append(e)
-                self._launch(e)
             peak_used, peak_active = max(peak_used, used), max(peak_active, len(active))
             progressed = False
             for e in list(active):
@@ -155,8 +171,12 @@ class Server:
                         e["plan"].close()
                         used -= e["bytes"]
                         active.remove(e)
-                    else:
-                        self._launch(e)
+            running = self._running_set(active)
+            peak_running = max(peak_running, len(running))
+            for e in running:
+                if not e["inflight"]:
+                    self._launch(e)
+                    progressed = True
             if not progressed:
                 time.sleep(2e-4)
         makespan = time.perf_counter() - t0
@@ -164,7 +184,8 @@ class Server:
         return {"requests": len(requests), "makespan_s": round(makespan, 3),
                 "solves_per_s": round(len(requests) / makespan, 4),
                 "ttr_p50_s": round(float(np.percentile(ttr, 50)), 3), "ttr_p99_s": round(float(np.percentile(ttr, 99)), 3),
-                "ttr_max_s": round(float(ttr.max()), 3), "peak_active": peak_active,
+                "ttr_max_s": round(float(ttr.max()), 3), "ttr_mean_s": round(float(ttr.mean()), 3),
+                "peak_active": peak_active, "peak_running": peak_running, "policy": self.policy,
                 "peak_bytes": int(peak_used), "budget_bytes": self.budget}
 
 
@@ -200,12 +221,14 @@ def main(argv=None):
     ap.add_argument("--chunk", type=int, default=25)
     ap.add_argument("--max-steps", type=int, default=2000)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--policy", default="srpt", choices=("srpt", "all"))
+    ap.add_argument("--fill-points", type=float, default=16e6)
     args = ap.parse_args(argv)
     from specter_gb300 import api
     free, total = api.device_memory()
     budget = int(args.budget_gb * 1e9) if args.budget_gb else int(0.8 * free)
     reqs = draw_requests(args.requests, args.rate, args.seed, steps=(100, args.max_steps))
-    srv = Server(budget, chunk=args.chunk)
+    srv = Server(budget, chunk=args.chunk, policy=args.policy, fill_points=int(args.fill_points))
     res = srv.run(reqs)
     res.update({"rate_per_s": args.rate, "seed": args.seed, "precision": "fp32-bulk", "chunk_steps": args.chunk,
                 "step_range": [100, args.max_steps]})

@@ -28,9 +28,9 @@ def test_results_same_alone_and_in_mix():
     from specter_gb300 import serve
     reqs = _requests()
     assert {r.kind for r in reqs} == {"HD", "BOUSS"}
-    srv = serve.Server(budget_bytes=8e9, chunk=7, keep_results=True)
+    srv = serve.Server(budget_bytes=8e9, chunk=7, keep_results=True, policy="all")
     stats = srv.run(reqs)
-    assert stats["peak_active"] >= 2  # requests overlapped on the device
+    assert stats["peak_running"] >= 2  # requests overlapped on the device
     for r in reqs:
         assert r.done > r.admitted >= 0
         for got, ref in zip(r.result, _alone(r)):
@@ -44,5 +44,16 @@ def test_budget_admission_serialises():
     stats = srv.run(reqs)
     assert stats["peak_active"] == 1
     for r in reqs[:2]:
+        for got, ref in zip(r.result, _alone(r)):
+            assert np.array_equal(got, ref)
+
+
+def test_srpt_policy_same_results():
+    from specter_gb300 import serve
+    reqs = _requests()
+    srv = serve.Server(budget_bytes=8e9, chunk=5, keep_results=True, policy="srpt", fill_points=1)
+    stats = srv.run(reqs)
+    assert stats["peak_running"] == 1 and stats["peak_active"] >= 2  # resident, run one at a time
+    for r in reqs:
         for got, ref in zip(r.result, _alone(r)):
             assert np.array_equal(got, ref)
