@@ -256,12 +256,11 @@ def main():
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
+    ptrs = [h.data_ptr() for h in host]
     for _ in range(Ke):
-        for f, h in zip(fields, host):
-            f.upload_ptr(h.data_ptr())
+        api.fields_upload(fields, ptrs)     # pinned host -> device, conversions overlapped
         s.step(1)
-        for f, h in zip(fields, host):
-            f.download_ptr(h.data_ptr())
+        api.fields_download(fields, ptrs)   # device -> pinned host, returns with the data on the host
     plan.synchronize()
     te = time.perf_counter() - t0
     te_t = torch.tensor([te], device=f"cuda:{local}")
@@ -285,7 +284,7 @@ def main():
                 "config": {"workload": f"BOUSS Rayleigh-Benard {cfg['nx']}x{cfg['ny']}x{cfg['nzp']} (+{cfg['cz']} FC-Gram, "
                                        f"NZ={cfg['nzp'] + cfg['cz']}), FP32-bulk, RK2, dt=1e-5",
                            "path": "reference-sequence" if args.refseq else "fused",
-                           "tile_caps_zyx_fused": list(caps) if caps else None,
+                           "autotune_caps_z_y_x_fused_split": list(caps) if caps else None,
                            "l2": f"inputs larger than L2 ({field_mb:.0f} MB per field), no flush",
                            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
                 "roofline": roof,

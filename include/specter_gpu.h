@@ -78,6 +78,11 @@ int specter_field_create(specter_plan *plan, int kind, specter_field **out);
 int specter_field_destroy(specter_field *f);
 int specter_field_upload(specter_field *f, const void *host);    /* reference layout */
 int specter_field_download(const specter_field *f, void *host);  /* reference layout */
+/* several fields of one plan (no reference counterpart): host copies on a copy stream overlap the
+ * layout conversions (two staging buffers).  Upload returns with the copies queued (host buffers
+ * must stay valid until the plan is synchronised); download returns with the data in host memory. */
+int specter_fields_upload(int n, specter_field *const *fields, const void *const *hosts);
+int specter_fields_download(int n, specter_field *const *fields, void *const *hosts);
 int specter_field_copy(specter_field *dst, const specter_field *src);
 int specter_field_zero(specter_field *f);
 /* upload/download of a contiguous batch of host rows is the same call with a pinned buffer;
@@ -161,7 +166,9 @@ int specter_solver_check(specter_solver *s);
 /* ---- autotuning and CUDA graphs (no reference counterpart: the ensemble and serving forms).
  * specter_solver_autotune times RK steps of the solver for each tile-width cap of the z, y, x
  *      and fused kernel families and keeps the fastest cap per family in the solver's plan; the
- *      state is restored afterwards.  caps (optional, 4 ints) receives the chosen caps.
+ *      state is restored afterwards; for fused solvers it also picks the one- or two-kernel
+ *      velocity stage.  caps (optional, 5 ints) receives the caps (z, y, x, fused) and the
+ *      velocity_split choice.
  * specter_plan_tile_caps sets the caps directly (entries <= 0 leave a cap unchanged).
  * specter_graph_create captures nsteps RK steps of n solvers into one CUDA graph: each
  *      solver's kernels stay on its plan stream, the chains of different plans are parallel
@@ -169,8 +176,11 @@ int specter_solver_check(specter_solver *s);
  *      plan streams and before work queued on them afterwards.  The solvers' own state fields
  *      are advanced in place.  Destroy a graph before its solvers. */
 typedef struct specter_graph specter_graph;
-int specter_solver_autotune(specter_solver *s, int caps[4]);
+int specter_solver_autotune(specter_solver *s, int caps[5]);
 int specter_plan_tile_caps(specter_plan *plan, const int caps[4]);
+/* named plan options: "velocity_split" (0/1: fused velocity stage as one kernel or as a
+ * per-component kernel plus a projection kernel), "tile_cap_z|y|x|fused" (1, 2, 4, 8, 16) */
+int specter_plan_set_option(specter_plan *plan, const char *name, int value);
 int specter_graph_create(specter_solver *const *solvers, int n, int nsteps, specter_graph **out);
 int specter_graph_launch(specter_graph *g);
 int specter_graph_synchronize(specter_graph *g);

@@ -31,10 +31,10 @@ EXPORTS = [
     "specter_s_imposebc",
     "specter_solver_create", "specter_solver_destroy", "specter_solver_fields", "specter_solver_step",
     "specter_solver_stage", "specter_solver_check",
-    "specter_solver_autotune", "specter_plan_tile_caps",
+    "specter_solver_autotune", "specter_plan_tile_caps", "specter_plan_set_option",
     "specter_graph_create", "specter_graph_launch", "specter_graph_synchronize", "specter_graph_kernels",
     "specter_graph_destroy", "specter_graph_query", "specter_solver_memory", "specter_device_memory",
-    "specter_table_check",
+    "specter_table_check", "specter_fields_upload", "specter_fields_download",
     "specter_timers", "specter_timers_reset",
     "specter_profile", "specter_profile_report", "specter_launch_count",
 ]
@@ -90,6 +90,7 @@ def load(path: str | None = None):
     L.specter_solver_stage.argtypes = [VP, C.c_int]
     L.specter_solver_autotune.argtypes = [VP, C.POINTER(C.c_int)]
     L.specter_plan_tile_caps.argtypes = [VP, C.POINTER(C.c_int)]
+    L.specter_plan_set_option.argtypes = [VP, C.c_char_p, C.c_int]
     L.specter_graph_create.argtypes = [C.POINTER(VP), C.c_int, C.c_int, C.POINTER(VP)]
     L.specter_graph_launch.argtypes = [VP]
     L.specter_graph_synchronize.argtypes = [VP]
@@ -99,6 +100,8 @@ def load(path: str | None = None):
     L.specter_solver_memory.argtypes = [VP, C.POINTER(C.c_ulonglong)]
     L.specter_device_memory.argtypes = [C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong)]
     L.specter_table_check.argtypes = [C.c_char_p, C.c_int, C.c_int, PD]
+    L.specter_fields_upload.argtypes = [C.c_int, C.POINTER(VP), C.POINTER(VP)]
+    L.specter_fields_download.argtypes = [C.c_int, C.POINTER(VP), C.POINTER(VP)]
     L.specter_field_create.argtypes = [VP, C.c_int, C.POINTER(VP)]
     L.specter_field_upload.argtypes = [VP, VP]
     L.specter_field_download.argtypes = [VP, VP]

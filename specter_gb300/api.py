@@ -356,9 +356,10 @@ class Solver:
         check(_L(self.plan).specter_solver_check(self.h))
 
     def autotune(self):
-        """Pick the tile-width caps of the plan's kernel families by timing RK steps of this
-        solver (state restored).  Returns the caps (z, y, x, fused)."""
-        caps = (C.c_int * 4)()
+        """Pick the tile-width caps of the plan's kernel families (and, for fused solvers, the
+        one- or two-kernel velocity stage) by timing RK steps of this solver (state restored).
+        Returns (z, y, x, fused caps, velocity_split)."""
+        caps = (C.c_int * 5)()
         check(_L(self.plan).specter_solver_autotune(self.h, caps))
         return tuple(caps)
 
@@ -369,6 +370,25 @@ def table_check(C_=25, d=5, tdir=None):
     out = (C.c_double * 3)()
     check(load().specter_table_check((tdir or TABLES).encode(), int(C_), int(d), out))
     return tuple(out)
+
+
+def fields_upload(fields, host_ptrs):
+    """Uploads several fields of one plan from host buffers (reference layout) given as
+    addresses; copies overlap the layout conversions.  Keep the buffers valid until the plan
+    is synchronised."""
+    n = len(fields)
+    f = (C.c_void_p * n)(*[x.h.value for x in fields])
+    h = (C.c_void_p * n)(*host_ptrs)
+    check(_L(fields[0].plan).specter_fields_upload(n, f, h))
+
+
+def fields_download(fields, host_ptrs):
+    """Downloads several fields of one plan into host buffers (reference layout); returns when
+    the data is in host memory."""
+    n = len(fields)
+    f = (C.c_void_p * n)(*[x.h.value for x in fields])
+    h = (C.c_void_p * n)(*host_ptrs)
+    check(_L(fields[0].plan).specter_fields_download(n, f, h))
 
 
 def device_memory():
@@ -383,6 +403,11 @@ def solver_memory(s: "Solver") -> int:
     b = C.c_ulonglong()
     check(_L(s.plan).specter_solver_memory(s.h, C.byref(b)))
     return b.value
+
+
+def set_option(plan: Plan, name: str, value: int):
+    """Named plan option (specter_plan_set_option): "velocity_split", "tile_cap_z" ..."""
+    check(_L(plan).specter_plan_set_option(plan.h, name.encode(), int(value)))
 
 
 def set_tile_caps(plan: Plan, caps):

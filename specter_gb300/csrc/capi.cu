@@ -214,10 +214,19 @@ __global__ void k_dev_to_ref(const V *__restrict__ d, V *__restrict__ h, int nz,
     }
 }
 
-static int staging(Plan &P, void **buf) {
-    // staging slot for reference-layout data: one more scratch field
-    *buf = P.scratch_field(23);
+static constexpr int kStageSlot = 23;  // scratch slots 23, 24: reference-layout staging
+
+static int staging(Plan &P, void **buf, int which = 0) {
+    *buf = P.scratch_field(kStageSlot + which);
     if (!*buf) { set_error("out of device memory (staging)"); return SPECTER_ERR_OOM; }
+    return SPECTER_OK;
+}
+
+static int xfer_init(Plan &P) {
+    if (P.copy_stream) return SPECTER_OK;
+    if (cudaStreamCreateWithFlags(&P.copy_stream, cudaStreamNonBlocking) != cudaSuccess) return check_launch("copy stream");
+    for (cudaEvent_t &e : P.xfer_ev)
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return check_launch("copy events");
     return SPECTER_OK;
 }
 
@@ -250,6 +259,70 @@ int specter_field_upload(specter_field *f, const void *host) {
     const size_t nbytes = (size_t)P.nz * P.ny * P.nxh * P.elt();
     if (cudaMemcpyAsync(stg, host, nbytes, cudaMemcpyHostToDevice, P.stream) != cudaSuccess) return check_launch("upload");
     return convert(P, stg, f->d, true);
+}
+
+// Several fields of one plan: host copies on the plan's copy stream overlap the layout
+// conversions on the plan stream, through two staging buffers (xfer_ev[b]: copy into / out of
+// buffer b done; xfer_ev[2 + b]: conversion from / into buffer b done).
+int specter_fields_upload(int n, specter_field *const *fields, const void *const *hosts) {
+    if (n < 1 || !fields || !hosts) { set_error("bad arguments"); return SPECTER_ERR_ARG; }
+    for (int i = 0; i < n; i++)
+        if (!fields[i] || !hosts[i] || fields[i]->plan != fields[0]->plan) { set_error("fields must share one plan"); return SPECTER_ERR_ARG; }
+    Plan &P = *fields[0]->plan->p;
+    int st = xfer_init(P);
+    if (st) return st;
+    cudaEventRecord(P.xfer_ev[2], P.stream);  // earlier work on the plan stream is ordered first
+    cudaStreamWaitEvent(P.copy_stream, P.xfer_ev[2], 0);
+    for (int i = 0; i < n; i++) {
+        specter_field *f = fields[i];
+        if (f->kind == SPECTER_REAL) {
+            if (cudaMemcpyAsync(f->d, hosts[i], f->bytes, cudaMemcpyHostToDevice, P.copy_stream) != cudaSuccess) return check_launch("upload");
+            cudaEventRecord(P.xfer_ev[0], P.copy_stream);
+            cudaStreamWaitEvent(P.stream, P.xfer_ev[0], 0);
+            continue;
+        }
+        const int b = i & 1;
+        void *stg;
+        if ((st = staging(P, &stg, b))) return st;
+        if (i >= 2) cudaStreamWaitEvent(P.copy_stream, P.xfer_ev[2 + b], 0);  // conversion i-2 left buffer b
+        const size_t nbytes = (size_t)P.nz * P.ny * P.nxh * P.elt();
+        if (cudaMemcpyAsync(stg, hosts[i], nbytes, cudaMemcpyHostToDevice, P.copy_stream) != cudaSuccess) return check_launch("upload");
+        cudaEventRecord(P.xfer_ev[b], P.copy_stream);
+        cudaStreamWaitEvent(P.stream, P.xfer_ev[b], 0);
+        if ((st = convert(P, stg, f->d, true))) return st;
+        cudaEventRecord(P.xfer_ev[2 + b], P.stream);
+    }
+    return check_launch("upload");
+}
+
+int specter_fields_download(int n, specter_field *const *fields, void *const *hosts) {
+    if (n < 1 || !fields || !hosts) { set_error("bad arguments"); return SPECTER_ERR_ARG; }
+    for (int i = 0; i < n; i++)
+        if (!fields[i] || !hosts[i] || fields[i]->plan != fields[0]->plan) { set_error("fields must share one plan"); return SPECTER_ERR_ARG; }
+    Plan &P = *fields[0]->plan->p;
+    int st = xfer_init(P);
+    if (st) return st;
+    for (int i = 0; i < n; i++) {
+        specter_field *f = fields[i];
+        const int b = i & 1;
+        if (f->kind == SPECTER_REAL) {
+            cudaEventRecord(P.xfer_ev[2 + b], P.stream);
+            cudaStreamWaitEvent(P.copy_stream, P.xfer_ev[2 + b], 0);
+            if (cudaMemcpyAsync(hosts[i], f->d, f->bytes, cudaMemcpyDeviceToHost, P.copy_stream) != cudaSuccess) return check_launch("download");
+            continue;
+        }
+        void *stg;
+        if ((st = staging(P, &stg, b))) return st;
+        if (i >= 2) cudaStreamWaitEvent(P.stream, P.xfer_ev[b], 0);  // copy-out i-2 left buffer b
+        if ((st = convert(P, f->d, stg, false))) return st;
+        cudaEventRecord(P.xfer_ev[2 + b], P.stream);
+        cudaStreamWaitEvent(P.copy_stream, P.xfer_ev[2 + b], 0);
+        const size_t nbytes = (size_t)P.nz * P.ny * P.nxh * P.elt();
+        if (cudaMemcpyAsync(hosts[i], stg, nbytes, cudaMemcpyDeviceToHost, P.copy_stream) != cudaSuccess) return check_launch("download");
+        cudaEventRecord(P.xfer_ev[b], P.copy_stream);
+    }
+    if (cudaStreamSynchronize(P.copy_stream) != cudaSuccess) return check_launch("download");
+    return SPECTER_OK;
 }
 
 int specter_field_download(const specter_field *f, void *host) {
@@ -582,7 +655,23 @@ int specter_plan_tile_caps(specter_plan *plan, const int caps[4]) {
     return SPECTER_OK;
 }
 
-int specter_solver_autotune(specter_solver *s, int caps[4]) {
+int specter_plan_set_option(specter_plan *plan, const char *name, int value) {
+    CHECK_PLAN(plan);
+    if (!name) { set_error("null option name"); return SPECTER_ERR_ARG; }
+    Plan &P = *plan->p;
+    if (!strcmp(name, "velocity_split")) { P.velocity_split = value ? 1 : 0; return SPECTER_OK; }
+    const char *caps[4] = {"tile_cap_z", "tile_cap_y", "tile_cap_x", "tile_cap_fused"};
+    for (int i = 0; i < 4; i++)
+        if (!strcmp(name, caps[i])) {
+            if (value < 1 || value > 16 || (value & (value - 1))) { set_error("tile caps are powers of two in [1, 16]"); return SPECTER_ERR_ARG; }
+            P.tile_cap[i] = value;
+            return SPECTER_OK;
+        }
+    set_error(std::string("unknown plan option ") + name);
+    return SPECTER_ERR_ARG;
+}
+
+int specter_solver_autotune(specter_solver *s, int caps[5]) {
     if (!s) { set_error("null solver"); return SPECTER_ERR_ARG; }
     Plan &P = *s->plan->p;
     if (P.profile) { set_error("autotune with profiling enabled"); return SPECTER_ERR_STATE; }
@@ -616,12 +705,22 @@ int specter_solver_autotune(specter_solver *s, int caps[4]) {
         // the state was advanced by the trials: bring it back before the next family
         if ((st = snap.put_back(s))) break;
     }
+    if (!st && s->fused) {  // fused velocity stage: two kernels or one
+        const int keep = P.velocity_split;
+        const float ms_keep = trial();
+        P.velocity_split = !keep;
+        const float ms_other = trial();
+        if (!(ms_other < ms_keep)) P.velocity_split = keep;
+        st = snap.put_back(s);
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (!st) st = snap.put_back(s);
     snap.release();
-    if (!st && caps)
+    if (!st && caps) {
         for (int i = 0; i < 4; i++) caps[i] = P.tile_cap[i];
+        caps[4] = P.velocity_split;
+    }
     return st;
 }
 

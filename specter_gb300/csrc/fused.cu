@@ -13,6 +13,7 @@ struct FusedState {
     void *X2[4] = {nullptr, nullptr, nullptr, nullptr};
     void *side = nullptr;  // theta rows of the kx = 0 and kx = nx/2 columns [2][ny][nzp]
     void *E[2] = {nullptr, nullptr};  // z spectra of the unit laplace_z profiles, per column
+    void *W[3] = {nullptr, nullptr, nullptr};  // split velocity form: updated components
     int nc = 3;
 };
 
@@ -108,6 +109,7 @@ int fused_create(Plan &P, const StageParams &sp, FusedState **out) {
     }
     if (sp.solver == 1) ok = ok && cudaMalloc(&fs->side, 2 * (size_t)P.ny * P.nzp * P.elt()) == cudaSuccess;  // BOUSS only
     for (int i = 0; i < 2; i++) ok = ok && cudaMalloc(&fs->E[i], P.field_bytes()) == cudaSuccess;
+    for (int i = 0; i < 3; i++) ok = ok && cudaMalloc(&fs->W[i], P.field_bytes()) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         fused_destroy(fs);
@@ -129,6 +131,7 @@ unsigned long long fused_bytes(const Plan &P, const FusedState *fs) {
     for (int i = 0; i < 4; i++) b += (fs->X1[i] ? P.field_bytes() : 0) + (fs->X2[i] ? P.field_bytes() : 0);
     b += fs->side ? 2ull * P.ny * P.nzp * P.elt() : 0;
     b += (fs->E[0] ? P.field_bytes() : 0) + (fs->E[1] ? P.field_bytes() : 0);
+    for (int i = 0; i < 3; i++) b += fs->W[i] ? P.field_bytes() : 0;
     return b;
 }
 
@@ -141,6 +144,8 @@ void fused_destroy(FusedState *fs) {
     if (fs->side) cudaFree(fs->side);
     for (int i = 0; i < 2; i++)
         if (fs->E[i]) cudaFree(fs->E[i]);
+    for (int i = 0; i < 3; i++)
+        if (fs->W[i]) cudaFree(fs->W[i]);
     delete fs;
 }
 
@@ -171,6 +176,7 @@ static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], c
     a.side = fs->side;
     a.hspec[0] = fs->E[0];
     a.hspec[1] = fs->E[1];
+    for (int i = 0; i < 3; i++) a.work[i] = fs->W[i];
     a.dt = sp.dt; a.nu = sp.nu; a.kappa = sp.kappa; a.rmp = 1 / (double)o;
     a.xmom = sp.xmom; a.xtemp = sp.xtemp;
     double tmp = 1 / (double)o;
@@ -184,7 +190,16 @@ static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], c
     // reads: NL (physical rows), vin, cold (+ theta for buoyancy), the two unit-profile
     // spectra; writes: vout and pr rows
     const double bv = row * (3.0 * P.nzp + (6.0 + (bouss ? 1 : 0) + 2.0) * P.nz + 3.0 * P.nz + P.nzp);
-    if ((st = launch<T>(P, a, kFusedVelocity, bv))) return st;
+    if (P.velocity_split) {
+        // part 1: NL, vin, cold (+ theta) in, the three updated components out; part 2: those
+        // and the unit-profile spectra in, vout and pr rows out
+        const double bc = row * (3.0 * P.nzp + (6.0 + (bouss ? 1 : 0)) * P.nz + 3.0 * P.nz);
+        const double bp = row * ((3.0 + 2.0) * P.nz + 3.0 * P.nz + P.nzp);
+        if ((st = launch<T>(P, a, kFusedVComp, bc))) return st;
+        if ((st = launch<T>(P, a, kFusedVProj, bp))) return st;
+    } else if ((st = launch<T>(P, a, kFusedVelocity, bv))) {
+        return st;
+    }
     if (bouss) {
         const double bt = row * (1.0 * P.nzp + 3.0 * P.nz + 1.0 * P.nz);
         if ((st = launch<T>(P, a, kFusedTheta, bt))) return st;

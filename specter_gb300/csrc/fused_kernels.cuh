@@ -31,6 +31,7 @@ struct FusedArgs {
     void *pr;             // pressure potential (mixed), walls read, rows [0, nzp) written
     void *side;           // theta rows of the kx = 0 and kx = nx/2 columns: [2][ny][nzp]
     const void *hspec[2]; // E1, E2: z spectra (with continuation) of the unit laplace_z profiles
+    void *work[3];        // split velocity form: the updated components between the two kernels
     double dt, nu, kappa, rmp, xmom, xtemp;
     double wall_tmp;      // 1/o, or (o+1)/o when o != ord (noslip_z)
     double vb[4];         // vxzsta, vyzsta, vxzend, vyzend
@@ -85,129 +86,140 @@ template <typename T>
 __device__ __forceinline__ double2 d2(C2<T> v) { return make_double2((double)v.x, (double)v.y); }
 
 // ----------------------------------------------------------------------------------------------
-// velocity column kernel: smem = U[3][nz][TK] + E::kBuffers * L * TK, plus small FP64 scratch
+// velocity: device functions shared by the one-block-per-tile kernel (k_fused_velocity) and the
+// split pair (k_fused_vcomp per component, k_fused_vproj for the projection)
 // ----------------------------------------------------------------------------------------------
-template <typename T, class E>
-__global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename E::Desc fd, FusedArgs a, int TK) {
-    const int lgTK = lg2(TK);
-    using V = C2<T>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int nz = g.nz, nzp = g.nzp, L = fd.L;
-    V *U = (V *)smem_raw;                       // 3 components, natural rows
-    V *X = U + (size_t)3 * nz * TK;             // FFT work
-    V *Y = X + (size_t)L * TK;
-    double2 *red = (double2 *)(X + (size_t)E::kBuffers * L * TK);  // [kThreads][2] partial wall sums
-    double2 *coef = red + 2 * kThreads;                             // [TK][2]
-    const int kx0 = blockIdx.x * TK, ky = blockIdx.y;
-    const int nv = min(TK, g.nxh - kx0);
-    auto colq = [&](int z, int c) { return fidx<T>(g, z, ky, kx0 + c); };
-    const T dt = (T)a.dt, nu = (T)a.nu, rmp = (T)a.rmp, xmom = (T)a.xmom, wall_tmp = (T)a.wall_tmp;
+struct ColTile {
+    int kx0, ky, nv, TK, lgTK;
+    size_t zs, col0;  // z stride of a column and the tile's first column offset
+};
 
-    // ---- 1. NL forward transforms, buoyancy, filter, laplak, RK update -> U[c].  Every HBM
-    //         read is an asynchronous tile copy: NL_{c+1} (or theta, for the buoyancy of
-    //         c = z) goes into the still unused slot U[c+1] while component c is transformed;
-    //         vin and cold go into the FFT buffer once the transformed NL has been consumed.
+template <typename T>
+__device__ __forceinline__ ColTile col_tile(const Geo &g, int TK) {
+    ColTile t;
+    t.TK = TK;
+    t.lgTK = lg2(TK);
+    t.kx0 = blockIdx.x * TK;
+    t.ky = blockIdx.y;
+    t.nv = min(TK, g.nxh - t.kx0);
+    t.zs = (size_t)g.ny * g.ldx;
+    t.col0 = (size_t)t.ky * g.ldx + t.kx0;
+    return t;
+}
+
+// Component c3 of the velocity update.  On entry X rows [0, nzp) hold NL_c3 (loads complete
+// for the calling thread) and, when buoy, a copy of theta's tile is in flight into Uc.  Forward
+// z transform with continuation, + 2 Om x v (ROTBOUSS), - xmom theta (buoy), fc_filter, then
+// Uc = cold + dt (nu lap(vin) - n) / o  (hd_rkstep2.f90:1-32, bouss_rkstep2.f90:1-48).
+template <typename T, class E>
+__device__ void vel_update(const Geo &g, const typename E::Desc &fd, const FusedArgs &a, const ColTile &t, int c3,
+                           C2<T> *Uc, C2<T> *X, C2<T> *Y, bool buoy) {
+    using V = C2<T>;
+    const int nz = g.nz, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
     const size_t tile = (size_t)nz * TK;
-    const size_t zs = (size_t)g.ny * g.ldx, col0 = (size_t)ky * g.ldx + kx0;
-    const bool stage2 = (size_t)E::kBuffers * L >= 2 * (size_t)nz;  // vin and cold both fit
-    for (int c3 = 0; c3 < 3; c3++) {
-        V *Uc = U + c3 * tile;
-        const bool buoy = c3 == 2 && a.bouss;
-        if (c3 == 0) {
-            tile_load_async(X, (const V *)a.nl[0] + col0, zs, nzp, TK, nv);
-            tile_load_async(U + tile, (const V *)a.nl[1] + col0, zs, nzp, TK, nv);
-            async_wait_n<1>();
-        } else {
-            async_wait();
-            __syncthreads();
-            for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Uc[idx];
-            __syncthreads();
-            if (c3 == 1) tile_load_async(U + 2 * tile, (const V *)a.nl[2] + col0, zs, nzp, TK, nv);
-            else if (buoy) tile_load_async(Uc, (const V *)a.vin[3] + col0, zs, nz, TK, nv);
-        }
-        __syncthreads();
-        fc_continuation<T>(g, X, TK);
-        __syncthreads();
-        V *R = E::run(X, Y, TK, fd, -1);
-        if (buoy) {
-            async_wait();
-            __syncthreads();
-        }
-        // (a) filtered nonlinear term (+ 2 Om x v, minus buoyancy) -> U[c]
-        const V *va = (const V *)a.vin[(c3 + 1) % 3], *vb = (const V *)a.vin[(c3 + 2) % 3];
-        const T oa = (T)a.omega[(c3 + 1) % 3], ob = (T)a.omega[(c3 + 2) % 3];
-        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
-            const int k = idx >> lgTK, c = idx & (TK - 1);
-            V n = mk<T>(0, 0);
-            if (c < nv) {
-                const int kx = kx0 + c;
-                n = R[E::pos(k, fd) * TK + c];
-                if (a.rot) {
-                    // component c of 2 Om x v = 2 (Om_a v_b - Om_b v_a), (c, a, b) cyclic
-                    const size_t q = colq(k, c);
-                    const V pa = va[q], pb = vb[q];
-                    n = mk<T>(n.x + (T)2 * (oa * pb.x - ob * pa.x), n.y + (T)2 * (oa * pb.y - ob * pa.y));
-                }
-                if (buoy) { const V t = Uc[idx]; n = mk<T>(n.x - xmom * t.x, n.y - xmom * t.y); }
-                n = cscale(n, g.FX<T>(kx));
-                n = cscale(n, g.FY<T>(ky));
-                n = cscale(n, g.FZ<T>(k));
-            }
-            Uc[idx] = n;
-        }
-        __syncthreads();
-        // (b) RK update with laplak of the stage input
-        const V *cold = (const V *)a.cold[c3];
-        tile_load_async(X, (const V *)a.vin[c3] + col0, zs, nz, TK, nv);
-        if (stage2) tile_load_async(X + tile, cold + col0, zs, nz, TK, nv);
+    const bool stage2 = (size_t)E::kBuffers * fd.L >= 2 * (size_t)nz;  // vin and cold both fit in X
+    const T dt = (T)a.dt, nu = (T)a.nu, rmp = (T)a.rmp, xmom = (T)a.xmom;
+    __syncthreads();
+    fc_continuation<T>(g, X, TK);
+    __syncthreads();
+    V *R = E::run(X, Y, TK, fd, -1);
+    if (buoy) {
         async_wait();
         __syncthreads();
-        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
-            const int k = idx >> lgTK, c = idx & (TK - 1);
-            if (c >= nv) { Uc[idx] = mk<T>(0, 0); continue; }
+    }
+    // (a) filtered nonlinear term (+ 2 Om x v, minus buoyancy) -> Uc
+    const V *va = (const V *)a.vin[(c3 + 1) % 3], *vb = (const V *)a.vin[(c3 + 2) % 3];
+    const T oa = (T)a.omega[(c3 + 1) % 3], ob = (T)a.omega[(c3 + 2) % 3];
+    for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+        const int k = idx >> lgTK, c = idx & (TK - 1);
+        V n = mk<T>(0, 0);
+        if (c < nv) {
             const int kx = kx0 + c;
-            const T k2 = g.KX<T>(kx) * g.KX<T>(kx) + g.KY<T>(ky) * g.KY<T>(ky) + g.KZ<T>(k) * g.KZ<T>(k);
-            const V v = X[idx], cv = stage2 ? X[tile + idx] : cold[colq(k, c)];
-            const V n = Uc[idx];
-            const V lap = cscale(v, -k2);
-            Uc[idx] = mk<T>(cv.x + dt * (nu * lap.x - n.x) * rmp, cv.y + dt * (nu * lap.y - n.y) * rmp);
-        }
-        __syncthreads();
-    }
-    // ---- 2. goto_domain_w_boundaries, noslip_z, goto_3d_fourier for vx, vy
-    const V *pr = (const V *)a.pr;
-    for (int c3 = 0; c3 < 2; c3++) {
-        V *Uc = U + (size_t)c3 * nz * TK;
-        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) X[idx] = Uc[idx];
-        __syncthreads();
-        V *R = E::run(X, Y, TK, fd, +1);
-        const T inz = (T)1 / (T)nz;
-        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
-            const int k = idx >> lgTK, c = idx & (TK - 1);
-            V v = cscale(R[E::pos(k, fd) * TK + c], inz);
-            if ((k == 0 || k == nzp - 1) && c < nv) {
-                const int kx = kx0 + c;
-                const V p = pr[colq(k, c)];
-                v = cscale(cimk(c3 == 0 ? g.KX<T>(kx) : g.KY<T>(ky), p), wall_tmp);
-                if (kx == 0 && ky == 0) v = mk<T>((T)((double)g.nx * g.ny * a.vb[(k == 0 ? 0 : 2) + c3]), (T)0);
+            n = R[E::pos(k, fd) * TK + c];
+            if (a.rot) {
+                // component c3 of 2 Om x v = 2 (Om_a v_b - Om_b v_a), (c3, a, b) cyclic
+                const size_t q = fidx<T>(g, k, ky, kx);
+                const V pa = va[q], pb = vb[q];
+                n = mk<T>(n.x + (T)2 * (oa * pb.x - ob * pa.x), n.y + (T)2 * (oa * pb.y - ob * pa.y));
             }
-            Uc[idx] = v;  // physical rows, natural order (temporary)
+            if (buoy) { const V th = Uc[idx]; n = mk<T>(n.x - xmom * th.x, n.y - xmom * th.y); }
+            n = cscale(n, g.FX<T>(kx));
+            n = cscale(n, g.FY<T>(ky));
+            n = cscale(n, g.FZ<T>(k));
         }
-        __syncthreads();
-        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Uc[idx];
-        __syncthreads();
-        fc_continuation<T>(g, X, TK);
-        __syncthreads();
-        R = E::run(X, Y, TK, fd, -1);
-        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
-            const int k = idx >> lgTK, c = idx & (TK - 1);
-            Uc[idx] = R[E::pos(k, fd) * TK + c];
-        }
-        __syncthreads();
+        Uc[idx] = n;
     }
-    // ---- 3. poisson_inhomogeneous: d -> X (natural), v -= i k d, wall sums of vz (FP64)
+    __syncthreads();
+    // (b) RK update with laplak of the stage input; vin (and cold) staged in the FFT buffer
+    const V *cold = (const V *)a.cold[c3];
+    tile_load_async(X, (const V *)a.vin[c3] + t.col0, t.zs, nz, TK, nv);
+    if (stage2) tile_load_async(X + tile, cold + t.col0, t.zs, nz, TK, nv);
+    async_wait();
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+        const int k = idx >> lgTK, c = idx & (TK - 1);
+        if (c >= nv) { Uc[idx] = mk<T>(0, 0); continue; }
+        const int kx = kx0 + c;
+        const T k2 = g.KX<T>(kx) * g.KX<T>(kx) + g.KY<T>(ky) * g.KY<T>(ky) + g.KZ<T>(k) * g.KZ<T>(k);
+        const V v = X[idx], cv = stage2 ? X[tile + idx] : cold[fidx<T>(g, k, ky, kx)];
+        const V n = Uc[idx];
+        const V lap = cscale(v, -k2);
+        Uc[idx] = mk<T>(cv.x + dt * (nu * lap.x - n.x) * rmp, cv.y + dt * (nu * lap.y - n.y) * rmp);
+    }
+    __syncthreads();
+}
+
+// goto_domain_w_boundaries, noslip_z, goto_3d_fourier for component c3 in {0, 1}
+// (boundary_mod.fpp:72-194, vboundary.f90:154-211): z-inverse, 1/nz on the physical rows, wall
+// rows from the previous stage's pressure, continuation and z-forward; Uc in and out.
+template <typename T, class E>
+__device__ void vel_walls(const Geo &g, const typename E::Desc &fd, const FusedArgs &a, const ColTile &t, int c3,
+                          C2<T> *Uc, C2<T> *X, C2<T> *Y) {
+    using V = C2<T>;
+    const int nz = g.nz, nzp = g.nzp, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
+    const V *pr = (const V *)a.pr;
+    const T wall_tmp = (T)a.wall_tmp, inz = (T)1 / (T)nz;
+    for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) X[idx] = Uc[idx];
+    __syncthreads();
+    V *R = E::run(X, Y, TK, fd, +1);
+    for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
+        const int k = idx >> lgTK, c = idx & (TK - 1);
+        V v = cscale(R[E::pos(k, fd) * TK + c], inz);
+        if ((k == 0 || k == nzp - 1) && c < nv) {
+            const int kx = kx0 + c;
+            const V p = pr[fidx<T>(g, k, ky, kx)];
+            v = cscale(cimk(c3 == 0 ? g.KX<T>(kx) : g.KY<T>(ky), p), wall_tmp);
+            if (kx == 0 && ky == 0) v = mk<T>((T)((double)g.nx * g.ny * a.vb[(k == 0 ? 0 : 2) + c3]), (T)0);
+        }
+        Uc[idx] = v;  // physical rows, natural order (temporary)
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Uc[idx];
+    __syncthreads();
+    fc_continuation<T>(g, X, TK);
+    __syncthreads();
+    R = E::run(X, Y, TK, fd, -1);
+    for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+        const int k = idx >> lgTK, c = idx & (TK - 1);
+        Uc[idx] = R[E::pos(k, fd) * TK + c];
+    }
+    __syncthreads();
+}
+
+// sol_project on the three updated components held in U (boundary_mod.fpp:197-448, 451-678):
+// Poisson, FP64 wall values of vz / nz and laplace_z coefficients, pressure IFFT(d)/nz + a(z),
+// harmonic correction from the precomputed unit-profile spectra, store of the new velocity.
+// red: [blockDim][2] double2, coef: [TK][2] double2 followed by TK LapCol<T>.
+template <typename T, class E>
+__device__ void vel_project(const Geo &g, const typename E::Desc &fd, const FusedArgs &a, const ColTile &t,
+                            C2<T> *U, C2<T> *X, C2<T> *Y, double2 *red, double2 *coef) {
+    using V = C2<T>;
+    const int nz = g.nz, nzp = g.nzp, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
+    const size_t tile = (size_t)nz * TK;
+    const bool stage2 = (size_t)E::kBuffers * fd.L >= 2 * (size_t)nz;
     const double2 *wtw = (const double2 *)g.wtw;
-    LapCol<T> *lcol = (LapCol<T> *)(coef + 2 * TK);  // [TK]
+    LapCol<T> *lcol = (LapCol<T> *)(coef + 2 * TK);
+    // ---- Poisson: d -> X (natural), v -= i k d, wall sums of vz (FP64)
     {
         const int c = threadIdx.x & (TK - 1), k0 = threadIdx.x >> lgTK, kstep = blockDim.x >> lgTK;
         const int kxc = min(kx0 + c, g.nxh - 1);
@@ -218,14 +230,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
                 const int idx = k * TK + c;
                 const T kz_ = g.KZ<T>(k);
                 const T k2 = kx_ * kx_ + ky_ * ky_ + kz_ * kz_;
-                V A = U[idx], B = U[(size_t)nz * TK + idx], Cc = U[(size_t)2 * nz * TK + idx];
+                V A = U[idx], B = U[tile + idx], Cc = U[2 * tile + idx];
                 const V s = mk<T>(kx_ * A.x + ky_ * B.x + kz_ * Cc.x, kx_ * A.y + ky_ * B.y + kz_ * Cc.y);
                 V D = mk<T>(s.y / k2, -s.x / k2);
                 if (k == 0 && ky == 0 && kx0 + c == 0) D = mk<T>(0, 0);
                 A = csub(A, cimk(kx_, D));
                 B = csub(B, cimk(ky_, D));
                 Cc = csub(Cc, cimk(kz_, D));
-                U[idx] = A; U[(size_t)nz * TK + idx] = B; U[(size_t)2 * nz * TK + idx] = Cc;
+                U[idx] = A; U[tile + idx] = B; U[2 * tile + idx] = Cc;
                 X[idx] = D;
                 const double vr = (double)Cc.x, vi = (double)Cc.y;
                 const double2 w = wtw[k];
@@ -241,8 +253,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
     if (threadIdx.x < TK) {
         const int c = threadIdx.x, kstep = blockDim.x >> lgTK;
         double2 b1 = make_double2(0, 0), b2 = make_double2(0, 0);
-        for (int t = 0; t < kstep; t++) {
-            const double2 p0 = red[2 * (t * TK + c)], p1 = red[2 * (t * TK + c) + 1];
+        for (int q = 0; q < kstep; q++) {
+            const double2 p0 = red[2 * (q * TK + c)], p1 = red[2 * (q * TK + c) + 1];
             b1.x += p0.x; b1.y += p0.y; b2.x += p1.x; b2.y += p1.y;
         }
         const double inz = 1.0 / nz;  // wall values of vz / nz
@@ -260,7 +272,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
         lcol[c] = lc;
     }
     __syncthreads();
-    // ---- 4. pressure: pr = IFFT_z(d)/nz + a(z) on the physical rows
+    // ---- pressure: pr = IFFT_z(d)/nz + a(z) on the physical rows
     {
         V *R = E::run(X, Y, TK, fd, +1);
         V *prw = (V *)a.pr;
@@ -271,24 +283,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
             V pa, pb;
             lap_profile_t<T>(lcol[c], g.ZZ<T>(k), Lz, pa, pb);
             const V dv = R[E::pos(k, fd) * TK + c];
-            prw[colq(k, c)] = mk<T>(dv.x * inz + pa.x, dv.y * inz + pa.y);
+            prw[fidx<T>(g, k, ky, kx0 + c)] = mk<T>(dv.x * inz + pa.x, dv.y * inz + pa.y);
         }
         __syncthreads();
     }
-    // ---- 5. harmonic correction: the spectra of a = c1 p1 + c2 p2 and b = da/dz are
-    //         c1 E1 + c2 E2 and kh (c1 E1 - c2 E2) (for kx = ky = 0: c1 E1 + c2 E2 and c1 E2,
-    //         real parts of c1, c2), E1, E2 precomputed per column
+    // ---- harmonic correction: the spectra of a = c1 p1 + c2 p2 and b = da/dz are
+    //      c1 E1 + c2 E2 and kh (c1 E1 - c2 E2) (for kx = ky = 0: c1 E1 + c2 E2 and c1 E2,
+    //      real parts of c1, c2), E1, E2 precomputed per column
     {
         const V *E1 = (const V *)a.hspec[0], *E2 = (const V *)a.hspec[1];
-        tile_load_async(X, E1 + col0, zs, nz, TK, nv);
-        if (stage2) tile_load_async(X + tile, E2 + col0, zs, nz, TK, nv);
+        tile_load_async(X, E1 + t.col0, t.zs, nz, TK, nv);
+        if (stage2) tile_load_async(X + tile, E2 + t.col0, t.zs, nz, TK, nv);
         async_wait();
         __syncthreads();
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
             const int k = idx >> lgTK, c = idx & (TK - 1);
             if (c >= nv) continue;
             const LapCol<T> lc = lcol[c];
-            const V e1 = X[idx], e2 = stage2 ? X[tile + idx] : E2[colq(k, c)];
+            const V e1 = X[idx], e2 = stage2 ? X[tile + idx] : E2[fidx<T>(g, k, ky, kx0 + c)];
             V A, B;
             if (lc.k0) {
                 A = mk<T>(lc.c1.x * e1.x + lc.c2.x * e2.x, lc.c1.x * e1.y + lc.c2.x * e2.y);
@@ -305,14 +317,99 @@ __global__ void __launch_bounds__(kThreads, 1) k_fused_velocity(Geo g, typename 
         }
         __syncthreads();
     }
-    // ---- 6. store the new velocity
+    // ---- store the new velocity
     for (int c3 = 0; c3 < 3; c3++) {
         V *vout = (V *)a.vout[c3];
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
             const int k = idx >> lgTK, c = idx & (TK - 1);
-            if (c < nv) vout[colq(k, c)] = U[(size_t)c3 * nz * TK + idx];
+            if (c < nv) vout[fidx<T>(g, k, ky, kx0 + c)] = U[c3 * tile + idx];
         }
     }
+}
+
+// One block per column tile for the whole velocity stage: smem = U[3][nz][TK] + FFT buffer(s)
+// + small FP64 scratch.  NL_{c+1} (or theta, for the buoyancy of c = z) is copied into the still
+// unused slot U[c+1] while component c is transformed.
+template <typename T, class E>
+__global__ void __launch_bounds__(E::kWideThreads, 1) k_fused_velocity(Geo g, typename E::Desc fd, FusedArgs a, int TK) {
+    using V = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nz = g.nz, nzp = g.nzp, L = fd.L;
+    const ColTile t = col_tile<T>(g, TK);
+    const size_t tile = (size_t)nz * TK;
+    V *U = (V *)smem_raw;                       // 3 components, natural rows
+    V *X = U + 3 * tile;                        // FFT work
+    V *Y = X + (size_t)L * TK;
+    double2 *red = (double2 *)(X + (size_t)E::kBuffers * L * TK);  // [blockDim][2] partial wall sums
+    double2 *coef = red + 2 * blockDim.x;                           // [TK][2] + LapCol[TK]
+    for (int c3 = 0; c3 < 3; c3++) {
+        V *Uc = U + c3 * tile;
+        const bool buoy = c3 == 2 && a.bouss;
+        if (c3 == 0) {
+            tile_load_async(X, (const V *)a.nl[0] + t.col0, t.zs, nzp, TK, t.nv);
+            tile_load_async(U + tile, (const V *)a.nl[1] + t.col0, t.zs, nzp, TK, t.nv);
+            async_wait_n<1>();
+        } else {
+            async_wait();
+            __syncthreads();
+            for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Uc[idx];
+            __syncthreads();
+            if (c3 == 1) tile_load_async(U + 2 * tile, (const V *)a.nl[2] + t.col0, t.zs, nzp, TK, t.nv);
+            else if (buoy) tile_load_async(Uc, (const V *)a.vin[3] + t.col0, t.zs, nz, TK, t.nv);
+        }
+        vel_update<T, E>(g, fd, a, t, c3, Uc, X, Y, buoy);
+    }
+    for (int c3 = 0; c3 < 2; c3++) vel_walls<T, E>(g, fd, a, t, c3, U + c3 * tile, X, Y);
+    vel_project<T, E>(g, fd, a, t, U, X, Y, red, coef);
+}
+
+// Split form, part 1: one block per (column tile, component): the component's update and, for
+// vx and vy, the wall round trip; the result goes to W[c] (a stage buffer).  smem = Uc[nz][TK] +
+// FFT buffer(s): half the footprint of k_fused_velocity, so two blocks share an SM.
+template <typename T, class E>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_vcomp(Geo g, typename E::Desc fd, FusedArgs a, int TK) {
+    using V = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nz = g.nz, nzp = g.nzp;
+    const ColTile t = col_tile<T>(g, TK);
+    const int c3 = blockIdx.z;
+    V *Uc = (V *)smem_raw;
+    V *X = Uc + (size_t)nz * TK;
+    V *Y = X + (size_t)fd.L * TK;
+    const bool buoy = c3 == 2 && a.bouss;
+    tile_load_async(X, (const V *)a.nl[c3] + t.col0, t.zs, nzp, TK, t.nv);
+    if (buoy) {
+        tile_load_async(Uc, (const V *)a.vin[3] + t.col0, t.zs, nz, TK, t.nv);
+        async_wait_n<1>();
+    } else {
+        async_wait();
+    }
+    vel_update<T, E>(g, fd, a, t, c3, Uc, X, Y, buoy);
+    if (c3 < 2) vel_walls<T, E>(g, fd, a, t, c3, Uc, X, Y);
+    V *w = (V *)a.work[c3];
+    for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+        const int k = idx >> t.lgTK, c = idx & (TK - 1);
+        if (c < t.nv) w[fidx<T>(g, k, t.ky, t.kx0 + c)] = Uc[idx];
+    }
+}
+
+// Split form, part 2: the projection of the three components written by k_fused_vcomp.
+template <typename T, class E>
+__global__ void __launch_bounds__(kThreads, 2) k_fused_vproj(Geo g, typename E::Desc fd, FusedArgs a, int TK) {
+    using V = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nz = g.nz;
+    const ColTile t = col_tile<T>(g, TK);
+    const size_t tile = (size_t)nz * TK;
+    V *U = (V *)smem_raw;
+    V *X = U + 3 * tile;
+    V *Y = X + (size_t)fd.L * TK;
+    double2 *red = (double2 *)(X + (size_t)E::kBuffers * fd.L * TK);
+    double2 *coef = red + 2 * blockDim.x;
+    for (int c3 = 0; c3 < 3; c3++) tile_load_async(U + c3 * tile, (const V *)a.work[c3] + t.col0, t.zs, nz, TK, t.nv);
+    async_wait();
+    __syncthreads();
+    vel_project<T, E>(g, fd, a, t, U, X, Y, red, coef);
 }
 
 // ----------------------------------------------------------------------------------------------

@@ -7,32 +7,49 @@
 
 namespace sg {
 
-enum FusedKernel { kFusedVelocity = 0, kFusedTheta = 1, kFusedHerm = 2 };
+enum FusedKernel { kFusedVelocity = 0, kFusedTheta = 1, kFusedHerm = 2, kFusedVComp = 3, kFusedVProj = 4 };
 
 template <typename T, class E>
 int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int which, double bytes) {
     const size_t es = sizeof(C2<T>);
     const size_t L = (size_t)fd.L;
     auto smem = [&](int tk) -> size_t {
-        if (which == kFusedVelocity)
-            return (3 * (size_t)P.nz + E::kBuffers * L) * tk * es + (2 * (size_t)kThreads + (size_t)tk * 2) * 16 +
+        if (which == kFusedVelocity || which == kFusedVProj) {
+            const size_t thr = which == kFusedVelocity ? (size_t)E::wide_threads(tk) : (size_t)kThreads;
+            return (3 * (size_t)P.nz + E::kBuffers * L) * tk * es + (2 * thr + (size_t)tk * 2) * 16 +
                    (size_t)tk * sizeof(LapCol<T>);
-        if (which == kFusedTheta) return ((size_t)P.nz + E::kBuffers * L) * tk * es;
+        }
+        if (which == kFusedTheta || which == kFusedVComp) return ((size_t)P.nz + E::kBuffers * L) * tk * es;
         return E::kBuffers * L * 2 * es;
     };
     int tk = 2;
     if (which != kFusedHerm) {
         tk = 0;
+        // the one-kernel velocity stage needs all three components: one block per SM; the others
+        // (including the projection, which holds the three components but transforms once) keep
+        // two blocks per SM
         const size_t budget = which == kFusedVelocity ? 200 * 1024 : 110 * 1024;
         for (int t : {16, 8, 4, 2, 1})
             if (t <= P.tile_cap[Plan::kTileFused] && smem(t) <= budget) { tk = t; break; }
         if (!tk) { set_error("z length too large for the fused column kernels"); return ERR_SHAPE; }
     }
     const size_t sm = smem(tk);
-    const char *name = which == kFusedVelocity ? "fused_velocity" : which == kFusedTheta ? "fused_theta" : "theta_herm";
+    const char *name = which == kFusedVelocity ? "fused_velocity"
+                       : which == kFusedTheta  ? "fused_theta"
+                       : which == kFusedVComp  ? "fused_vcomp"
+                       : which == kFusedVProj  ? "fused_vproj"
+                                               : "theta_herm";
     P.prof_begin(name, bytes);
     if (which == kFusedVelocity) {
         auto k = k_fused_velocity<T, E>;
+        if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k<<<dim3(cdiv(P.nxh, tk), P.ny), E::wide_threads(tk), sm, P.stream>>>(P.geo, fd, a, tk);
+    } else if (which == kFusedVComp) {
+        auto k = k_fused_vcomp<T, E>;
+        if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        k<<<dim3(cdiv(P.nxh, tk), P.ny, 3), kThreads, sm, P.stream>>>(P.geo, fd, a, tk);
+    } else if (which == kFusedVProj) {
+        auto k = k_fused_vproj<T, E>;
         if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k<<<dim3(cdiv(P.nxh, tk), P.ny), kThreads, sm, P.stream>>>(P.geo, fd, a, tk);
     } else if (which == kFusedTheta) {

@@ -33,6 +33,8 @@ struct GenericFFT {
     using Desc = FFTDesc;
     static constexpr int kBuffers = 2;
     static constexpr int kMinBlocks = 1;
+    static constexpr int kWideThreads = kThreads;
+    static int wide_threads(int) { return kThreads; }
     static __device__ __forceinline__ C2<T> *run(C2<T> *X, C2<T> *Y, int B, const Desc &d, int sign) {
         return fft_exec<T>(X, Y, B, d, sign);
     }
@@ -49,6 +51,16 @@ struct FourStep {
     using Desc = FFT4Desc;
     static constexpr int kBuffers = 1;
     static constexpr int kMinBlocks = 2;  // cap registers at 128 so two blocks share an SM
+    // Kernels that run one block per SM (the fused velocity kernel) may take enough threads for
+    // one item per thread in both steps at a tile width of 8: 8 * max(L1, L2) rounded up to a
+    // warp, at least kThreads.  With 36 x 30 that is 288, so the 288 items of step B do not leave
+    // a one-warp second round behind a barrier.
+    static constexpr int kWideThreads =
+        (8 * (L1 > L2 ? L1 : L2) + 31) / 32 * 32 > kThreads ? (8 * (L1 > L2 ? L1 : L2) + 31) / 32 * 32 : kThreads;
+    static int wide_threads(int tk) {
+        const int need = (tk * (L1 > L2 ? L1 : L2) + 31) / 32 * 32;
+        return need > kThreads && need <= kWideThreads ? need : kThreads;
+    }
     static __device__ __forceinline__ C2<T> *run(C2<T> *X, C2<T> *, int B, const Desc &d, int sign) {
         if constexpr (OUTLINE) {
             if (d.blue) fft4_bluestein_ni<T, L1, L2>(X, B, d, sign);

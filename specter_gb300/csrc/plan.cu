@@ -373,6 +373,9 @@ void plan_destroy(Plan *p) {
     if (p->dred) cudaFree(p->dred);
     if (p->dwtw) cudaFree(p->dwtw);
     if (p->hred) cudaFreeHost(p->hred);
+    if (p->copy_stream) { cudaStreamSynchronize(p->copy_stream); cudaStreamDestroy(p->copy_stream); }
+    for (cudaEvent_t e : p->xfer_ev)
+        if (e) cudaEventDestroy(e);
     if (p->stream) cudaStreamDestroy(p->stream);
     delete p;
 }

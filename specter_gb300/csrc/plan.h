@@ -72,6 +72,10 @@ struct Plan {
     FFTTable tx, ty, tz;      // lengths H = nx/2, ny, nz
     FFT4Table tx4, ty4, tz4;  // four-step tables of the same lengths (FP32 plans)
     cudaStream_t stream = nullptr;
+    // host transfers of several fields: copies on their own stream, double-buffered staging
+    // (scratch slots kStageSlot, kStageSlot + 1) and events ordering copies with conversions
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t xfer_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     Geo geo{};
     // scratch (lazily allocated, complex fields / small buffers)
     std::vector<void *> scratch;
@@ -88,6 +92,8 @@ struct Plan {
     // column kernels), set by the autotuner; a launcher uses min(cap, largest width that fits).
     enum { kTileZ = 0, kTileY = 1, kTileX = 2, kTileFused = 3 };
     int tile_cap[4] = {16, 16, 16, 16};
+    // fused velocity stage as two kernels (per-component update, then the projection) or one
+    int velocity_split = 1;
     int capped(int t, int kind) const { return t < tile_cap[kind] ? t : tile_cap[kind]; }
     long long launches = 0;
     bool profile = false;

@@ -51,7 +51,7 @@ def test_autotune_keeps_state_and_results():
     p2, s2 = _solver(api, initial, 48, 48, 65, 1, seed=3)
     before = _state(s1)
     caps = s1.autotune()
-    assert len(caps) == 4 and all(c in (1, 2, 4, 8, 16) for c in caps)
+    assert len(caps) == 5 and all(c in (1, 2, 4, 8, 16) for c in caps[:4]) and caps[4] in (0, 1)
     for x, y in zip(before, _state(s1)):
         assert np.array_equal(x, y)
     # tile widths change the launch shape, not the per-column arithmetic (only the grouping of

@@ -176,10 +176,12 @@ OMEGA = (0.3, -0.7, 2.0)
 
 
 @pytest.mark.parametrize("solver", [0, 1, 2], ids=["HD", "BOUSS", "ROTBOUSS"])
-@pytest.mark.parametrize("fused", [False, True], ids=["refseq", "fused"])
+@pytest.mark.parametrize("fused", [False, True, "one-kernel"], ids=["refseq", "fused", "fused1"])
 def test_rk_step(pair, solver, fused):
     from specter_gb300 import api
     plan, g = pair
+    api.set_option(plan, "velocity_split", 0 if fused == "one-kernel" else 1)
+    fused = bool(fused)
     rng = np.random.default_rng(8 + solver)
     v = [smooth_spectral(g, rng, amp=0.3) for _ in range(3)]
     th = smooth_spectral(g, rng, amp=0.3)
@@ -199,3 +201,26 @@ def test_rk_step(pair, solver, fused):
         assert rel(a, b) < 1e-11
     nzp = g.nz - g.cz
     assert rel(s.pr.download()[:, :, :nzp], ref[-1][:, :, :nzp]) < 1e-8
+
+
+def test_fields_batched_transfer():
+    """specter_fields_upload / specter_fields_download move several fields like the single-field
+    calls (pipelined through two staging buffers)."""
+    from specter_gb300 import api
+    plan = api.Plan((24, 16, 40), (0, 0, 25), (0, 0, 5), (1.0, 1.0, 1.0), precision=1)
+    rng = np.random.default_rng(3)
+    data = [(rng.standard_normal(plan.sshape) + 1j * rng.standard_normal(plan.sshape)).astype(np.complex64)
+            for _ in range(5)]
+    fields = [plan.field() for _ in range(5)]
+    api.fields_upload(fields, [d.ctypes.data for d in data])
+    plan.synchronize()
+    for f, d in zip(fields, data):
+        assert np.array_equal(f.download(), d)
+    out = [np.empty_like(d) for d in data]
+    for f in fields:
+        f.zero()
+    for f, d in zip(fields, data):
+        f.upload(d)
+    api.fields_download(fields, [o.ctypes.data for o in out])
+    for o, d in zip(out, data):
+        assert np.array_equal(o, d)
