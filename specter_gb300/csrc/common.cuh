@@ -57,11 +57,11 @@ __device__ __forceinline__ void async_wait_n() { asm volatile("cp.async.wait_gro
 // src[k*stride + c] for c < nv and is zero for nv <= c < TK.  Call async_wait() and
 // __syncthreads() before reading the tile.
 template <typename V>
-__device__ __forceinline__ void tile_load_async(V *dst, const V *src, size_t stride, int rows, int TK, int nv) {
+__device__ __forceinline__ void tile_load_async(V *dst, const V *src, unsigned stride, int rows, int TK, int nv) {
     const int lgTK = lg2(TK);
     for (int idx = threadIdx.x; idx < rows * TK; idx += blockDim.x) {
         const int k = idx >> lgTK, c = idx & (TK - 1);
-        if (c < nv) cp_async<sizeof(V)>(dst + idx, src + (size_t)k * stride + c);
+        if (c < nv) cp_async<sizeof(V)>(dst + idx, src + ((unsigned)k * stride + (unsigned)c));
         else { V z; z.x = 0; z.y = 0; dst[idx] = z; }
     }
     async_commit();
@@ -71,13 +71,13 @@ __device__ __forceinline__ void tile_load_async(V *dst, const V *src, size_t str
 // dst[k*dstride + c], comes from src[c*cstride + k] (c < nv), so consecutive threads read
 // consecutive k.  An odd dstride (TK + 1) keeps those shared-memory writes free of bank conflicts.
 template <typename V>
-__device__ __forceinline__ void rows_load_async(V *dst, const V *src, size_t cstride, int rows, int TK, int nv,
+__device__ __forceinline__ void rows_load_async(V *dst, const V *src, unsigned cstride, int rows, int TK, int nv,
                                                 int dstride) {
     // (c, k) = divmod(idx, rows), advanced by blockDim.x without dividing per element
     const int sc = blockDim.x / rows, sk = blockDim.x - sc * rows;
     int c = threadIdx.x / rows, k = threadIdx.x - c * rows;
     for (int idx = threadIdx.x; idx < rows * TK; idx += blockDim.x) {
-        if (c < nv) cp_async<sizeof(V)>(dst + k * dstride + c, src + (size_t)c * cstride + k);
+        if (c < nv) cp_async<sizeof(V)>(dst + k * dstride + c, src + ((unsigned)c * cstride + (unsigned)k));
         else { V z; z.x = 0; z.y = 0; dst[k * dstride + c] = z; }
         c += sc;
         k += sk;

@@ -152,7 +152,7 @@ int zinv(Plan &P, const ZInvArgs &a0, int nf, double bytes) {
     const size_t sm = per * tk;
     smem_attr(k_z_inverse<float, E>, sm);
     Scope s(P, "z_inverse", bytes);
-    k_z_inverse<float, E><<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz4.d, a, tk);
+    k_z_inverse<float, E><<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz4.d, a.prepared(), tk);
     return done("z_inverse");
 }
 
@@ -163,7 +163,7 @@ int zfwd(Plan &P, const ZFwdArgs &a, int nf, double bytes) {
     const size_t sm = (size_t)P.tz4.d.L * tk * sizeof(float2);
     smem_attr(k_z_forward<float, E>, sm);
     Scope s(P, "z_forward", bytes);
-    k_z_forward<float, E><<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz4.d, a, tk);
+    k_z_forward<float, E><<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz4.d, a.prepared(), tk);
     return done("z_forward");
 }
 
@@ -177,7 +177,7 @@ int ypass(Plan &P, const YArgs &a0, int nf, int nplanes, double bytes) {
     const size_t sm = per * tk;
     smem_attr(k_y_pass<float, E>, sm);
     Scope s(P, a.sign < 0 ? "y_forward" : "y_inverse", bytes);
-    k_y_pass<float, E><<<dim3(cdiv(P.nxh, tk), nplanes, nf), kThreads, sm, P.stream>>>(P.geo, P.ty4.d, a, tk);
+    k_y_pass<float, E><<<dim3(cdiv(P.nxh, tk), nplanes, nf), kThreads, sm, P.stream>>>(P.geo, P.ty4.d, a.prepared(), tk);
     return done("y_pass");
 }
 
@@ -193,11 +193,11 @@ int xpass(Plan &P, const XArgs &a, int nf, bool r2c, double bytes) {
     if (r2c) {
         smem_attr(k_x_r2c<float, E>, sm);
         Scope s(P, "x_r2c", bytes);
-        k_x_r2c<float, E><<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a, rb);
+        k_x_r2c<float, E><<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a.prepared(), rb);
     } else {
         smem_attr(k_x_c2r<float, E>, sm);
         Scope s(P, "x_c2r", bytes);
-        k_x_c2r<float, E><<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a, rb);
+        k_x_c2r<float, E><<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a.prepared(), rb);
     }
     return done(r2c ? "x_r2c" : "x_c2r");
 }
@@ -212,7 +212,7 @@ int xnl(Plan &P, const XNLArgs &a, double bytes) {
     const size_t sm = x_nl_elems<E>(P.tx4.d, P.nxh, P.H, rb) * sizeof(float2);
     smem_attr(k_x_nonlinear<float, E>, sm);
     Scope s(P, "x_nonlinear", bytes);
-    k_x_nonlinear<float, E><<<dim3(cdiv(a.nrows * P.ny, rb)), kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a, rb);
+    k_x_nonlinear<float, E><<<dim3(cdiv(a.nrows * P.ny, rb)), kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a.prepared(), rb);
     return done("x_nonlinear");
 }
 }  // namespace

@@ -38,6 +38,14 @@ struct FusedArgs {
     double omega[3];      // rotation rate (rot != 0)
     int bouss;
     int rot;              // ROTBOUSS: Coriolis term, no final theta filter / round trip
+    float f_dt, f_nu, f_kappa, f_rmp, f_xmom, f_xtemp, f_wall_tmp, f_omega[3];  // FP32 mirrors
+    FusedArgs prepared() const {
+        FusedArgs b = *this;
+        b.f_dt = (float)dt; b.f_nu = (float)nu; b.f_kappa = (float)kappa; b.f_rmp = (float)rmp;
+        b.f_xmom = (float)xmom; b.f_xtemp = (float)xtemp; b.f_wall_tmp = (float)wall_tmp;
+        for (int i = 0; i < 3; i++) b.f_omega[i] = (float)omega[i];
+        return b;
+    }
 };
 
 // Per-column laplace_z parameters in the kernel's precision: kh = |(kx, ky)| and the
@@ -75,9 +83,8 @@ __device__ __forceinline__ void lap_coef_neumann(const Geo &g, int kx, int ky, d
         c2 = make_double2(0.0, 0.0);
         return;
     }
-    const double kh = sqrt(g.kx[kx] * g.kx[kx] + g.ky[ky] * g.ky[ky]);
-    const double e = exp(-(kh * g.Lz));
-    const double tmp = 1.0 / (kh * (1 - exp(-(2 * kh * g.Lz))));
+    const double *lc = g.lapc + ((size_t)ky * g.nxh + kx) * 3;  // kh, exp(-kh Lz), 1/(kh (1 - exp(-2 kh Lz)))
+    const double e = lc[1], tmp = lc[2];
     c1 = make_double2((b2.x - b1.x * e) * tmp, (b2.y - b1.y * e) * tmp);
     c2 = make_double2((-b1.x + b2.x * e) * tmp, (-b1.y + b2.y * e) * tmp);
 }
@@ -91,7 +98,7 @@ __device__ __forceinline__ double2 d2(C2<T> v) { return make_double2((double)v.x
 // ----------------------------------------------------------------------------------------------
 struct ColTile {
     int kx0, ky, nv, TK, lgTK;
-    size_t zs, col0;  // z stride of a column and the tile's first column offset
+    unsigned zs, col0;  // z stride of a column and the tile's first column offset
 };
 
 template <typename T>
@@ -102,8 +109,8 @@ __device__ __forceinline__ ColTile col_tile(const Geo &g, int TK) {
     t.kx0 = blockIdx.x * TK;
     t.ky = blockIdx.y;
     t.nv = min(TK, g.nxh - t.kx0);
-    t.zs = (size_t)g.ny * g.ldx;
-    t.col0 = (size_t)t.ky * g.ldx + t.kx0;
+    t.zs = (unsigned)g.ny * g.ldx;
+    t.col0 = (unsigned)t.ky * g.ldx + t.kx0;
     return t;
 }
 
@@ -116,9 +123,10 @@ __device__ void vel_update(const Geo &g, const typename E::Desc &fd, const Fused
                            C2<T> *Uc, C2<T> *X, C2<T> *Y, bool buoy) {
     using V = C2<T>;
     const int nz = g.nz, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
-    const size_t tile = (size_t)nz * TK;
+    const int tile = nz * TK;
     const bool stage2 = (size_t)E::kBuffers * fd.L >= 2 * (size_t)nz;  // vin and cold both fit in X
-    const T dt = (T)a.dt, nu = (T)a.nu, rmp = (T)a.rmp, xmom = (T)a.xmom;
+    const T dt = pick<T>(a.dt, a.f_dt), nu = pick<T>(a.nu, a.f_nu), rmp = pick<T>(a.rmp, a.f_rmp);
+    const T xmom = pick<T>(a.xmom, a.f_xmom);
     __syncthreads();
     fc_continuation<T>(g, X, TK);
     __syncthreads();
@@ -129,7 +137,8 @@ __device__ void vel_update(const Geo &g, const typename E::Desc &fd, const Fused
     }
     // (a) filtered nonlinear term (+ 2 Om x v, minus buoyancy) -> Uc
     const V *va = (const V *)a.vin[(c3 + 1) % 3], *vb = (const V *)a.vin[(c3 + 2) % 3];
-    const T oa = (T)a.omega[(c3 + 1) % 3], ob = (T)a.omega[(c3 + 2) % 3];
+    const T oa = pick<T>(a.omega[(c3 + 1) % 3], a.f_omega[(c3 + 1) % 3]);
+    const T ob = pick<T>(a.omega[(c3 + 2) % 3], a.f_omega[(c3 + 2) % 3]);
     for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
         const int k = idx >> lgTK, c = idx & (TK - 1);
         V n = mk<T>(0, 0);
@@ -138,7 +147,7 @@ __device__ void vel_update(const Geo &g, const typename E::Desc &fd, const Fused
             n = R[E::pos(k, fd) * TK + c];
             if (a.rot) {
                 // component c3 of 2 Om x v = 2 (Om_a v_b - Om_b v_a), (c3, a, b) cyclic
-                const size_t q = fidx<T>(g, k, ky, kx);
+                const unsigned q = fidx<T>(g, k, ky, kx);
                 const V pa = va[q], pb = vb[q];
                 n = mk<T>(n.x + (T)2 * (oa * pb.x - ob * pa.x), n.y + (T)2 * (oa * pb.y - ob * pa.y));
             }
@@ -178,7 +187,7 @@ __device__ void vel_walls(const Geo &g, const typename E::Desc &fd, const FusedA
     using V = C2<T>;
     const int nz = g.nz, nzp = g.nzp, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
     const V *pr = (const V *)a.pr;
-    const T wall_tmp = (T)a.wall_tmp, inz = (T)1 / (T)nz;
+    const T wall_tmp = pick<T>(a.wall_tmp, a.f_wall_tmp), inz = (T)1 / (T)nz;
     for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) X[idx] = Uc[idx];
     __syncthreads();
     V *R = E::run(X, Y, TK, fd, +1);
@@ -215,7 +224,7 @@ __device__ void vel_project(const Geo &g, const typename E::Desc &fd, const Fuse
                             C2<T> *U, C2<T> *X, C2<T> *Y, double2 *red, double2 *coef) {
     using V = C2<T>;
     const int nz = g.nz, nzp = g.nzp, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
-    const size_t tile = (size_t)nz * TK;
+    const int tile = nz * TK;
     const bool stage2 = (size_t)E::kBuffers * fd.L >= 2 * (size_t)nz;
     const double2 *wtw = (const double2 *)g.wtw;
     LapCol<T> *lcol = (LapCol<T> *)(coef + 2 * TK);
@@ -246,14 +255,25 @@ __device__ void vel_project(const Geo &g, const typename E::Desc &fd, const Fuse
                 s1.y += vr * w.y + vi * w.x;
             }
         }
-        red[2 * threadIdx.x] = s0;
-        red[2 * threadIdx.x + 1] = s1;
+        // sum over the threads of a column: shuffles within each warp (the lanes of column c are
+        // c, c + TK, ...), then one partial per warp
+        for (int off = TK; off < 32; off <<= 1) {
+            s0.x += __shfl_xor_sync(0xffffffffu, s0.x, off);
+            s0.y += __shfl_xor_sync(0xffffffffu, s0.y, off);
+            s1.x += __shfl_xor_sync(0xffffffffu, s1.x, off);
+            s1.y += __shfl_xor_sync(0xffffffffu, s1.y, off);
+        }
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (lane < TK) {
+            red[2 * (warp * TK + lane)] = s0;
+            red[2 * (warp * TK + lane) + 1] = s1;
+        }
     }
     __syncthreads();
     if (threadIdx.x < TK) {
-        const int c = threadIdx.x, kstep = blockDim.x >> lgTK;
+        const int c = threadIdx.x, nwarps = blockDim.x >> 5;
         double2 b1 = make_double2(0, 0), b2 = make_double2(0, 0);
-        for (int q = 0; q < kstep; q++) {
+        for (int q = 0; q < nwarps; q++) {
             const double2 p0 = red[2 * (q * TK + c)], p1 = red[2 * (q * TK + c) + 1];
             b1.x += p0.x; b1.y += p0.y; b2.x += p1.x; b2.y += p1.y;
         }
@@ -265,7 +285,7 @@ __device__ void vel_project(const Geo &g, const typename E::Desc &fd, const Fuse
         coef[2 * c] = c1;
         coef[2 * c + 1] = c2;
         LapCol<T> lc;
-        lc.kh = (T)sqrt(g.kx[kxc] * g.kx[kxc] + g.ky[ky] * g.ky[ky]);
+        lc.kh = (T)g.lapc[((size_t)ky * g.nxh + kxc) * 3];
         lc.c1 = mk<T>((T)c1.x, (T)c1.y);
         lc.c2 = mk<T>((T)c2.x, (T)c2.y);
         lc.k0 = kxc == 0 && ky == 0;
@@ -336,7 +356,7 @@ __global__ void __launch_bounds__(E::kWideThreads, 1) k_fused_velocity(Geo g, ty
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nz = g.nz, nzp = g.nzp, L = fd.L;
     const ColTile t = col_tile<T>(g, TK);
-    const size_t tile = (size_t)nz * TK;
+    const int tile = nz * TK;
     V *U = (V *)smem_raw;                       // 3 components, natural rows
     V *X = U + 3 * tile;                        // FFT work
     V *Y = X + (size_t)L * TK;
@@ -400,7 +420,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_fused_vproj(Geo g, typename E::
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nz = g.nz;
     const ColTile t = col_tile<T>(g, TK);
-    const size_t tile = (size_t)nz * TK;
+    const int tile = nz * TK;
     V *U = (V *)smem_raw;
     V *X = U + 3 * tile;
     V *Y = X + (size_t)fd.L * TK;
@@ -427,11 +447,12 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
     const int kx0 = blockIdx.x * TK, ky = blockIdx.y;
     const int nv = min(TK, g.nxh - kx0);
     auto colq = [&](int z, int c) { return fidx<T>(g, z, ky, kx0 + c); };
-    const T dt = (T)a.dt, kap = (T)a.kappa, rmp = (T)a.rmp, inz = (T)1 / (T)nz, xtemp = (T)a.xtemp;
+    const T dt = pick<T>(a.dt, a.f_dt), kap = pick<T>(a.kappa, a.f_kappa), rmp = pick<T>(a.rmp, a.f_rmp);
+    const T inz = (T)1 / (T)nz, xtemp = pick<T>(a.xtemp, a.f_xtemp);
     // 1. NL_theta forward, heat current, filter, laplak, update.  vz is copied into Th while
     //    NL_theta is transformed; theta and cold go into the FFT buffer afterwards.
     {
-        const size_t tile = (size_t)nz * TK;
+        const int tile = nz * TK;
         const size_t zs = (size_t)g.ny * g.ldx, col0 = (size_t)ky * g.ldx + kx0;
         const bool stage2 = (size_t)E::kBuffers * L >= 2 * (size_t)nz;
         tile_load_async(X, (const V *)a.nl[3] + col0, zs, nzp, TK, nv);
@@ -521,7 +542,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
             Th[idx] = v;
             const int kx = kx0 + c;
             if (c < nv && (kx == 0 || kx == g.nxh - 1))
-                side[((size_t)(kx == 0 ? 0 : 1) * g.ny + ky) * nzp + k] = v;
+                side[((unsigned)(kx == 0 ? 0 : 1) * g.ny + ky) * nzp + k] = v;
         }
         __syncthreads();
         for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Th[idx];

@@ -23,9 +23,20 @@ namespace sg {
 constexpr int kThreads = 256;
 constexpr int kMaxF = 4;  // fields per launch (blockIdx.z)
 
+// element offset in a field; fields hold fewer than 2^32 elements (checked at plan creation), so
+// offsets stay 32-bit (64-bit multiplies per element cost several instructions)
 template <typename T>
-__device__ __forceinline__ size_t fidx(const Geo &g, int z, int ky, int kx) {
-    return ((size_t)z * g.ny + ky) * g.ldx + kx;
+__device__ __forceinline__ unsigned fidx(const Geo &g, int z, int ky, int kx) {
+    return ((unsigned)z * (unsigned)g.ny + (unsigned)ky) * (unsigned)g.ldx + (unsigned)kx;
+}
+
+// A double kernel parameter in the kernel's precision.  FP32 kernels read the float mirror that
+// the launcher fills (Args::prepared()): converting the double inside a kernel running at its
+// register cap gets rematerialised per element on the FP64 pipe (1/64 rate here).
+template <typename T>
+__device__ __forceinline__ T pick(double d, float f) {
+    if constexpr (sizeof(T) == 8) return d;
+    else return f;
 }
 
 template <typename T>
@@ -100,6 +111,8 @@ struct ZInvArgs {
     int scale_rows;   // rows [0, scale_rows) scaled, the rest copied unscaled
     double scale;
     int staged;       // 1: the input tile is staged once in smem (some field has two outputs)
+    float scale_f;
+    ZInvArgs prepared() const { ZInvArgs b = *this; b.scale_f = (float)scale; return b; }
 };
 
 template <typename T, class E>
@@ -112,9 +125,9 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_inverse(Geo g, ty
     const int kx0 = blockIdx.x * TK, ky = blockIdx.y, f = blockIdx.z;
     const V *in = (const V *)a.in[f];
     const int nv = min(TK, g.nxh - kx0);
-    const size_t zstride = (size_t)g.ny * g.ldx;
-    const V *src = in + (size_t)ky * g.ldx + kx0;
-    const T sc = (T)a.scale;
+    const unsigned zstride = (unsigned)g.ny * g.ldx;
+    const V *src = in + (unsigned)ky * g.ldx + kx0;
+    const T sc = pick<T>(a.scale, a.scale_f);
     if (a.staged) tile_load_async(S, src, zstride, g.nz, TK, nv);
     for (int pass = 1; pass >= 0; pass--) {  // derivative output first: out0 may alias in
         V *out = (V *)(pass == 0 ? a.out0[f] : a.out1[f]);
@@ -142,7 +155,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_inverse(Geo g, ty
             if (c >= nv) continue;
             V v = R[E::pos(k, fd) * TK + c];
             if (k < a.scale_rows) v = cscale(v, sc);
-            const size_t q = fidx<T>(g, k, ky, kx0 + c);
+            const unsigned q = fidx<T>(g, k, ky, kx0 + c);
             if (pass == 0 && add) v = cadd(v, add[q]);
             out[q] = v;
         }
@@ -159,6 +172,8 @@ struct ZFwdArgs {
     const void *in[kMaxF];
     void *out[kMaxF];
     double in_scale;
+    float in_scale_f;
+    ZFwdArgs prepared() const { ZFwdArgs b = *this; b.in_scale_f = (float)in_scale; return b; }
 };
 
 template <typename T>
@@ -192,8 +207,8 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_forward(Geo g, ty
     const V *in = (const V *)a.in[f];
     V *out = (V *)a.out[f];
     const int nv = min(TK, g.nxh - kx0);
-    const T s = (T)a.in_scale;
-    tile_load_async(X, in + (size_t)ky * g.ldx + kx0, (size_t)g.ny * g.ldx, g.nzp, TK, nv);
+    const T s = pick<T>(a.in_scale, a.in_scale_f);
+    tile_load_async(X, in + (unsigned)ky * g.ldx + kx0, (unsigned)g.ny * g.ldx, g.nzp, TK, nv);
     async_wait();
     if (a.in_scale != 1.0) {
         __syncthreads();
@@ -219,6 +234,8 @@ struct YArgs {
     int sign;
     double scale;
     int staged;       // 1: the input tile is staged once in smem (some field has two outputs)
+    float scale_f;
+    YArgs prepared() const { YArgs b = *this; b.scale_f = (float)scale; return b; }
 };
 
 template <typename T, class E>
@@ -231,10 +248,10 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass(Geo g, typen
     const int kx0 = blockIdx.x * TK, z = blockIdx.y, f = blockIdx.z;
     const V *in = (const V *)a.in[f];
     const int nv = min(TK, g.nxh - kx0);
-    const T sc = (T)a.scale;
-    const bool scaled = a.scale != 1.0;
-    const V *src = in + (size_t)z * g.ny * g.ldx + kx0;
-    if (a.staged) tile_load_async(S, src, (size_t)g.ldx, g.ny, TK, nv);
+    const T sc = pick<T>(a.scale, a.scale_f);
+    const bool scaled = sizeof(T) == 8 ? a.scale != 1.0 : a.scale_f != 1.0f;
+    const V *src = in + (unsigned)z * g.ny * g.ldx + kx0;
+    if (a.staged) tile_load_async(S, src, (unsigned)g.ldx, g.ny, TK, nv);
     for (int pass = 1; pass >= 0; pass--) {  // derivative output first: out0 may alias in
         V *out = (V *)(pass == 0 ? a.out0[f] : a.out1[f]);
         if (!out) continue;
@@ -246,7 +263,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass(Geo g, typen
                 X[idx] = pass == 1 ? cimk(g.KY<T>(idx >> lgTK), v) : v;
             }
         } else {
-            tile_load_async(X, src, (size_t)g.ldx, g.ny, TK, nv);
+            tile_load_async(X, src, (unsigned)g.ldx, g.ny, TK, nv);
             async_wait();
             if (pass == 1) {
                 __syncthreads();
@@ -323,12 +340,12 @@ __device__ __forceinline__ void r2c_post(const Geo &g, const typename E::Desc &f
 
 // shared [rows][SP] staging -> rows of a global array (row stride ld), rows < nv
 template <typename V>
-__device__ __forceinline__ void rows_store(V *out, size_t ld, const V *S, int rows, int SP, int nv) {
+__device__ __forceinline__ void rows_store(V *out, unsigned ld, const V *S, int rows, int SP, int nv) {
     // (r, k) = divmod(idx, rows), advanced by blockDim.x without dividing per element
     const int sr = blockDim.x / rows, sk = blockDim.x - sr * rows;
     int r = threadIdx.x / rows, k = threadIdx.x - r * rows;
     for (int idx = threadIdx.x; idx < rows * nv; idx += blockDim.x) {
-        out[(size_t)r * ld + k] = S[k * SP + r];
+        out[(unsigned)r * ld + k] = S[k * SP + r];
         r += sr;
         k += sk;
         if (k >= rows) { k -= rows; r++; }
@@ -341,6 +358,8 @@ struct XArgs {
     void *out[kMaxF];
     int nrows;  // z planes
     double scale;
+    float scale_f;
+    XArgs prepared() const { XArgs b = *this; b.scale_f = (float)scale; return b; }
 };
 
 // shared memory of the x pass kernels: FFT buffer(s) + staging, for RB rows
@@ -363,7 +382,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_r2c(Geo g, typena
     V *out = (V *)a.out[f];
     const int H = g.H;
     // packed real row: element m = (x_{2m}, x_{2m+1})
-    rows_load_async(S, (const V *)(in + (size_t)row0 * g.nx), (size_t)H, H, RB, nv, SP);
+    rows_load_async(S, (const V *)(in + (size_t)row0 * g.nx), (unsigned)H, H, RB, nv, SP);
     async_wait();
     __syncthreads();
     for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) X[idx] = S[(idx >> lgRB) * SP + (idx & (RB - 1))];
@@ -372,12 +391,12 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_r2c(Geo g, typena
     r2c_post<T, E>(g, fd, R, S, RB, SP);
     __syncthreads();
     if (a.scale != 1.0) {
-        const T sc = (T)a.scale;
-    const bool scaled = a.scale != 1.0;
+        const T sc = pick<T>(a.scale, a.scale_f);
+    const bool scaled = sizeof(T) == 8 ? a.scale != 1.0 : a.scale_f != 1.0f;
         for (int idx = threadIdx.x; idx < g.nxh * SP; idx += blockDim.x) S[idx] = cscale(S[idx], sc);
     }
     __syncthreads();
-    rows_store(out + (size_t)row0 * g.ldx, (size_t)g.ldx, S, g.nxh, SP, nv);
+    rows_store(out + (size_t)row0 * g.ldx, (unsigned)g.ldx, S, g.nxh, SP, nv);
 }
 
 // x pass C2R: r[row] = IFFT_x(in[row]) (Hermitian half spectrum; Im of kx=0, nx/2 ignored)
@@ -393,15 +412,15 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_c2r(Geo g, typena
     const int nv = min(RB, nrows - row0);
     const V *in = (const V *)a.in[f];
     T *out = (T *)a.out[f];
-    rows_load_async(S, in + (size_t)row0 * g.ldx, (size_t)g.ldx, g.nxh, RB, nv, SP);
+    rows_load_async(S, in + (size_t)row0 * g.ldx, (unsigned)g.ldx, g.nxh, RB, nv, SP);
     async_wait();
     __syncthreads();
     c2r_pre<T>(g, S, X, RB, SP);
     __syncthreads();
     V *R = E::run(X, Y, RB, fd, +1);
     const int H = g.H;
-    const T sc = (T)a.scale;
-    const bool scaled = a.scale != 1.0;
+    const T sc = pick<T>(a.scale, a.scale_f);
+    const bool scaled = sizeof(T) == 8 ? a.scale != 1.0 : a.scale_f != 1.0f;
     for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
         const int m = idx >> lgRB, r = idx & (RB - 1);
         V v = R[E::pos(m, fd) * RB + r];
@@ -409,7 +428,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_c2r(Geo g, typena
         S[m * SP + r] = v;
     }
     __syncthreads();
-    rows_store((V *)(out + (size_t)row0 * g.nx), (size_t)H, S, H, SP, nv);
+    rows_store((V *)(out + (size_t)row0 * g.nx), (unsigned)H, S, H, SP, nv);
 }
 
 // ---------------------------------------------------------------------------------
@@ -429,6 +448,8 @@ struct XNLArgs {
     int c0, c1;          // components [c0, c1) are formed (0..2 velocity, 3 scalar)
     int nrows;           // physical z planes
     double tmp;          // 1/(nx ny nz)^2
+    float tmp_f;
+    XNLArgs prepared() const { XNLArgs b = *this; b.tmp_f = (float)tmp; return b; }
 };
 
 // Input t of the nonlinear x pass: t < 3 the velocity rows; then per component i in [c0, c1)
@@ -468,10 +489,10 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, 
     const int row0 = blockIdx.x * RB, nrows = a.nrows * g.ny;
     const int nv = min(RB, nrows - row0);
     const int T_in = 3 + 3 * nc;
-    const T tmp = (T)a.tmp;
+    const T tmp = pick<T>(a.tmp, a.tmp_f);
     const size_t off = (size_t)row0 * g.ldx;
     int term, i;
-    rows_load_async(S, xnl_input<T>(a, 0, term, i) + off, (size_t)g.ldx, nxh, RB, nv, SP);
+    rows_load_async(S, xnl_input<T>(a, 0, term, i) + off, (unsigned)g.ldx, nxh, RB, nv, SP);
     for (int t = 0; t < T_in; t++) {
         xnl_input<T>(a, t, term, i);
         async_wait();
@@ -480,7 +501,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, 
         __syncthreads();  // S is free
         if (term != 2 && t + 1 < T_in) {
             int tn, in_;
-            rows_load_async(S, xnl_input<T>(a, t + 1, tn, in_) + off, (size_t)g.ldx, nxh, RB, nv, SP);
+            rows_load_async(S, xnl_input<T>(a, t + 1, tn, in_) + off, (unsigned)g.ldx, nxh, RB, nv, SP);
         }
         V *R = E::run(X, Y, RB, fd, +1);
         if (term < 2) {
@@ -488,12 +509,12 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, 
                 const int m = idx >> lgRB, r = idx & (RB - 1);
                 const V p = R[E::pos(m, fd) * RB + r];
                 if (term < 0) {
-                    U[(size_t)i * H * RB + idx] = p;
+                    U[i * H * RB + idx] = p;
                 } else if (term == 0) {
                     const V u = U[idx];
                     A[idx] = mk<T>(u.x * p.x, u.y * p.y);
                 } else {
-                    const V u = U[(size_t)H * RB + idx];
+                    const V u = U[H * RB + idx];
                     A[idx] = mk<T>(A[idx].x + u.x * p.x, A[idx].y + u.y * p.y);
                 }
             }
@@ -502,18 +523,18 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, 
             for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
                 const int m = idx >> lgRB, r = idx & (RB - 1);
                 const int q = E::pos(m, fd) * RB + r;
-                const V u = U[(size_t)2 * H * RB + idx], p = R[q], acc = A[idx];
+                const V u = U[2 * H * RB + idx], p = R[q], acc = A[idx];
                 R[q] = mk<T>((acc.x + u.x * p.x) * tmp, (acc.y + u.y * p.y) * tmp);
             }
             __syncthreads();
             V *Z = E::run_perm(R, R == X ? Y : X, RB, fd, -1);
             r2c_post<T, E, true>(g, fd, Z, S, RB, SP);
             __syncthreads();
-            rows_store((V *)a.out[i] + off, (size_t)g.ldx, S, nxh, SP, nv);
+            rows_store((V *)a.out[i] + off, (unsigned)g.ldx, S, nxh, SP, nv);
             if (t + 1 < T_in) {
                 __syncthreads();
                 int tn, in_;
-                rows_load_async(S, xnl_input<T>(a, t + 1, tn, in_) + off, (size_t)g.ldx, nxh, RB, nv, SP);
+                rows_load_async(S, xnl_input<T>(a, t + 1, tn, in_) + off, (unsigned)g.ldx, nxh, RB, nv, SP);
             }
         }
     }

@@ -88,7 +88,7 @@ static int launch_z_inverse(Plan &P, const ZInvArgs &a0, int nf) {
     if (fst != kNoFast) return fst;
     set_smem(k_z_inverse<T, GenericFFT<T>>, sm);
     Launch L(P, "z_inverse", bytes);
-    k_z_inverse<T, GenericFFT<T>><<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz.d, a, tk);
+    k_z_inverse<T, GenericFFT<T>><<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz.d, a.prepared(), tk);
     return check_launch("z_inverse");
 }
 
@@ -103,7 +103,7 @@ static int launch_z_forward(Plan &P, const ZFwdArgs &a, int nf) {
     if (fst != kNoFast) return fst;
     set_smem(k_z_forward<T, GenericFFT<T>>, sm);
     Launch L(P, "z_forward", bytes);
-    k_z_forward<T, GenericFFT<T>><<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz.d, a, tk);
+    k_z_forward<T, GenericFFT<T>><<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz.d, a.prepared(), tk);
     return check_launch("z_forward");
 }
 
@@ -121,7 +121,7 @@ static int launch_y(Plan &P, const YArgs &a0, int nf, int nplanes) {
     if (fst != kNoFast) return fst;
     set_smem(k_y_pass<T, GenericFFT<T>>, sm);
     Launch L(P, a.sign < 0 ? "y_forward" : "y_inverse", bytes);
-    k_y_pass<T, GenericFFT<T>><<<dim3(cdiv(P.nxh, tk), nplanes, nf), kThreads, sm, P.stream>>>(P.geo, P.ty.d, a, tk);
+    k_y_pass<T, GenericFFT<T>><<<dim3(cdiv(P.nxh, tk), nplanes, nf), kThreads, sm, P.stream>>>(P.geo, P.ty.d, a.prepared(), tk);
     return check_launch("y_pass");
 }
 
@@ -141,11 +141,11 @@ static int launch_x(Plan &P, const XArgs &a, int nf, bool r2c) {
     if (r2c) {
         set_smem(k_x_r2c<T, GenericFFT<T>>, sm);
         Launch L(P, "x_r2c", bytes);
-        k_x_r2c<T, GenericFFT<T>><<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx.d, a, rb);
+        k_x_r2c<T, GenericFFT<T>><<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx.d, a.prepared(), rb);
     } else {
         set_smem(k_x_c2r<T, GenericFFT<T>>, sm);
         Launch L(P, "x_c2r", bytes);
-        k_x_c2r<T, GenericFFT<T>><<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx.d, a, rb);
+        k_x_c2r<T, GenericFFT<T>><<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx.d, a.prepared(), rb);
     }
     return check_launch(r2c ? "x_r2c" : "x_c2r");
 }
@@ -166,7 +166,7 @@ static int launch_x_nl(Plan &P, const XNLArgs &a) {
     if (fst != kNoFast) return fst;
     set_smem(k_x_nonlinear<T, GenericFFT<T>>, sm);
     Launch L(P, "x_nonlinear", bytes);
-    k_x_nonlinear<T, GenericFFT<T>><<<dim3(cdiv(a.nrows * P.ny, rb)), kThreads, sm, P.stream>>>(P.geo, P.tx.d, a, rb);
+    k_x_nonlinear<T, GenericFFT<T>><<<dim3(cdiv(a.nrows * P.ny, rb)), kThreads, sm, P.stream>>>(P.geo, P.tx.d, a.prepared(), rb);
     return check_launch("x_nonlinear");
 }
 

@@ -210,6 +210,12 @@ int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], cons
     p->nxh = nx / 2 + 1; p->nzp = nz - c[2]; p->H = nx / 2;
     p->ldx = (p->nxh + 7) / 8 * 8;
     p->Lx = len[0]; p->Ly = len[1]; p->Lz = len[2];
+    // kernels index fields with 32-bit offsets
+    if ((double)nz * ny * (((nx / 2 + 1) + 7) / 8 * 8) >= 4294967296.0 || (double)nx * ny * nz >= 4294967296.0) {
+        set_error("grid too large: a field must hold fewer than 2^32 elements");
+        delete p;
+        return ERR_SHAPE;
+    }
     int st = load_tables(p, tdir ? tdir : ".");
     if (st) { delete p; return st; }
     // grids and wavenumbers, src/specter.fpp:683-800
@@ -273,6 +279,23 @@ int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], cons
     G.kxf = p->dgeof + okx; G.kyf = p->dgeof + oky; G.kzf = p->dgeof + okz; G.zf = p->dgeof + oz_;
     G.fxf = p->dgeof + ofx; G.fyf = p->dgeof + ofy; G.fzf = p->dgeof + ofz;
     G.xtw = p->dxtw;
+    {
+        // laplace_z constants of every (kx, ky) column (boundary_mod.fpp:521-549)
+        std::vector<double> lc((size_t)3 * ny * p->nxh, 0.0);
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < p->nxh; i++) {
+                const double kh = std::sqrt(p->kx[i] * p->kx[i] + p->ky[j] * p->ky[j]);
+                double *c = &lc[((size_t)j * p->nxh + i) * 3];
+                c[0] = kh;
+                if (i || j) {
+                    c[1] = std::exp(-(kh * p->Lz));
+                    c[2] = 1.0 / (kh * (1 - std::exp(-(2 * kh * p->Lz))));
+                }
+            }
+        if (cudaMalloc(&p->dlapc, lc.size() * sizeof(double)) != cudaSuccess) { set_error("cudaMalloc failed"); plan_destroy(p); return ERR_OOM; }
+        cudaMemcpy(p->dlapc, lc.data(), lc.size() * sizeof(double), cudaMemcpyHostToDevice);
+        G.lapc = p->dlapc;
+    }
     p->nred = 4096;
     cudaMalloc(&p->dred, sizeof(double) * p->nred);
     {
@@ -369,6 +392,7 @@ void plan_destroy(Plan *p) {
     free_fft4_table(p->tx4); free_fft4_table(p->ty4); free_fft4_table(p->tz4);
     if (p->dgeo) cudaFree(p->dgeo);
     if (p->dgeof) cudaFree(p->dgeof);
+    if (p->dlapc) cudaFree(p->dlapc);
     if (p->dxtw) cudaFree(p->dxtw);
     if (p->dred) cudaFree(p->dred);
     if (p->dwtw) cudaFree(p->dwtw);

@@ -44,6 +44,7 @@ struct Geo {
     const double *fx, *fy, *fz;               // fc_filter factors per axis (FP64)
     const float *kxf, *kyf, *kzf, *zf;         // the same tables rounded to FP32, so FP32
     const float *fxf, *fyf, *fzf;             // kernels do no FP64 conversion per element
+    const double *lapc;                       // per (ky, kx) column: kh, exp(-kh Lz), Neumann 1/(kh (1 - exp(-2 kh Lz)))
     const void *xtw;                          // C2<T>[H+1]: exp(-2*pi*i*k/nx)
     const void *wtw;                          // double2[nz]: exp(+2*pi*i*k*(nzp-1)/nz)
     double Lz;
@@ -68,6 +69,7 @@ struct Plan {
     std::vector<double> kx, ky, kz, z, dir, fx, fy, fz;
     double *dgeo = nullptr;   // device block holding kx, ky, kz, z, dir, fx, fy, fz
     float *dgeof = nullptr;   // the same block rounded to FP32
+    double *dlapc = nullptr;  // laplace_z column constants (Geo::lapc)
     void *dxtw = nullptr;
     FFTTable tx, ty, tz;      // lengths H = nx/2, ny, nz
     FFT4Table tx4, ty4, tz4;  // four-step tables of the same lengths (FP32 plans)
