@@ -249,14 +249,15 @@ def main():
     # end to end: state uploaded from pinned host memory and downloaded every step
     fields = [f for f in (s.vx, s.vy, s.vz, s.th, s.pr)]
     host = [torch.empty(f.nbytes, dtype=torch.uint8, pin_memory=True) for f in fields]
-    for f, h in zip(fields, host):
-        f.download_ptr(h.data_ptr())
-    Ke = max(2, K // 2)
+    ptrs = [h.data_ptr() for h in host]
+    # one untimed round trip creates the staging buffers and the copy stream
+    api.fields_download(fields, ptrs)
+    api.fields_upload(fields, ptrs)
+    Ke = max(3, K // 2)
     plan.synchronize()
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
-    ptrs = [h.data_ptr() for h in host]
     for _ in range(Ke):
         api.fields_upload(fields, ptrs)     # pinned host -> device, conversions overlapped
         s.step(1)

@@ -127,7 +127,7 @@ int stage_tile(void *const out0[], void *const out1[], int nf, int L, int n) {
 
 template <typename K>
 void smem_attr(K kern, size_t bytes) {
-    if (bytes > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (bytes > 40 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 struct Scope {

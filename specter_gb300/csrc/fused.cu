@@ -81,7 +81,7 @@ static int harmonic_spectra(Plan &P, void *E1, void *E2) {
     else {
         const size_t sm = 2 * (size_t)t->d.L * tk * es;
         auto k = k_z_forward<double, GenericFFT<double>>;
-        if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k<<<dim3(cdiv(P.nxh, tk), P.ny, 2), kThreads, sm, P.stream>>>(P.geo, t->d, a, tk);
         if (P.prec != FP64) {
             k_narrow<<<152 * 8, 256, 0, P.stream>>>(p1, (float2 *)E1, n);

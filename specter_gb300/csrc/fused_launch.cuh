@@ -42,23 +42,23 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
     P.prof_begin(name, bytes);
     if (which == kFusedVelocity) {
         auto k = k_fused_velocity<T, E>;
-        if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k<<<dim3(cdiv(P.nxh, tk), P.ny), E::wide_threads(tk), sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
     } else if (which == kFusedVComp) {
         auto k = k_fused_vcomp<T, E>;
-        if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k<<<dim3(cdiv(P.nxh, tk), P.ny, 3), kThreads, sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
     } else if (which == kFusedVProj) {
         auto k = k_fused_vproj<T, E>;
-        if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k<<<dim3(cdiv(P.nxh, tk), P.ny), kThreads, sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
     } else if (which == kFusedTheta) {
         auto k = k_fused_theta<T, E>;
-        if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k<<<dim3(cdiv(P.nxh, tk), P.ny), kThreads, sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
     } else {
         auto k = k_theta_herm<T, E>;
-        if (sm > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k<<<dim3(P.ny, 2), kThreads, sm, P.stream>>>(P.geo, fd, a.prepared());
     }
     P.prof_end();

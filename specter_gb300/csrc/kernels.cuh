@@ -176,22 +176,36 @@ struct ZFwdArgs {
     ZFwdArgs prepared() const { ZFwdArgs b = *this; b.in_scale_f = (float)in_scale; return b; }
 };
 
+constexpr int kMaxOz = 9;   // largest d of the FC-Gram tables (Q3 .. Q9)
+constexpr int kMaxTile = 16; // largest tile width of the column passes
+
+// Called by every thread of the block with X rows [0, nzp) filled and visible; returns with the
+// continuation rows written (visible after the caller's next barrier).
 template <typename T>
 __device__ __forceinline__ void fc_continuation(const Geo &g, C2<T> *X, int TK) {
+    // the 2d wall-adjacent values of each column in FP64, converted once per column rather than
+    // once per continued row: wv[j][c] = row nzp-d+j (j < d), row d-1-(j-d) (j >= d)
+    __shared__ double2 wv[2 * kMaxOz * kMaxTile];
     const int lgTK = lg2(TK);
-    // X holds rows [0, nzp) of TK columns; fill rows [nzp, nz)
     const int C = g.cz, d = g.oz, n = g.nz;
+    for (int idx = threadIdx.x; idx < 2 * d * TK; idx += blockDim.x) {
+        const int j = idx >> lgTK, c = idx & (TK - 1);
+        const int row = j < d ? n - C - d + j : d - 1 - (j - d);
+        const C2<T> v = X[row * TK + c];
+        wv[idx] = make_double2((double)v.x, (double)v.y);
+    }
+    __syncthreads();
     for (int idx = threadIdx.x; idx < C * TK; idx += blockDim.x) {
         const int ii = idx >> lgTK, c = idx & (TK - 1);
-        const C2<T> t0 = X[(n - C - d) * TK + c], b0 = X[(d - 1) * TK + c];
+        const double2 t0 = wv[c], b0 = wv[d * TK + c];
         const double a0 = __ldg(g.dir + ii), a1 = __ldg(g.dir + (C - 1 - ii));
-        double ar = a0 * (double)t0.x + a1 * (double)b0.x;
-        double ai = a0 * (double)t0.y + a1 * (double)b0.y;
+        double ar = a0 * t0.x + a1 * b0.x;
+        double ai = a0 * t0.y + a1 * b0.y;
         for (int jj = 1; jj < d; jj++) {
-            const C2<T> t = X[(n - C - d + jj) * TK + c], b = X[(d - 1 - jj) * TK + c];
+            const double2 t = wv[jj * TK + c], b = wv[(d + jj) * TK + c];
             const double w0 = __ldg(g.dir + ii + C * jj), w1 = __ldg(g.dir + (C - 1 - ii) + C * jj);
-            ar = ar + w0 * (double)t.x + w1 * (double)b.x;
-            ai = ai + w0 * (double)t.y + w1 * (double)b.y;
+            ar = ar + w0 * t.x + w1 * b.x;
+            ai = ai + w0 * t.y + w1 * b.y;
         }
         X[(n - C + ii) * TK + c] = mk<T>((T)ar, (T)ai);
     }

@@ -38,9 +38,11 @@ static int pick_tile(size_t per_col_bytes) {
     return 0;
 }
 
+// Opt in to more than the default 48 KB per block early: kernels that run the FC-Gram
+// continuation also hold a small static array (fc_continuation), which counts against it.
 template <typename K>
 static void set_smem(K kern, size_t bytes) {
-    if (bytes > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (bytes > 40 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 static int elem_blocks(const Plan &P, int rows) {

@@ -198,6 +198,10 @@ int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], cons
         set_error("only periodic x,y with an FC-Gram z direction is supported (Cx=Cy=ox=oy=0)");
         return ERR_SHAPE;
     }
+    if (o[2] > 9) {  // the continuation kernels hold at most 2 * 9 wall-adjacent rows per column
+        set_error("oz > 9 is not supported (the FC-Gram tables stop at d = 9)");
+        return ERR_SHAPE;
+    }
     if (nx < 4 || ny < 2 || nz < 4 || nx % 2 || ny % 2 || nz % 2 || c[2] <= 0 || o[2] <= 0 ||
         nz - c[2] < 2 * o[2] || nz - c[2] < 2) {
         set_error("bad grid shape: nx, ny, nz must be even, nz - Cz >= 2*oz");

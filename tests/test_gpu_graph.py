@@ -54,13 +54,20 @@ def test_autotune_keeps_state_and_results():
     assert len(caps) == 5 and all(c in (1, 2, 4, 8, 16) for c in caps[:4]) and caps[4] in (0, 1)
     for x, y in zip(before, _state(s1)):
         assert np.array_equal(x, y)
-    # tile widths change the launch shape, not the per-column arithmetic (only the grouping of
-    # the FP64 wall sums, whose rounding can move an FP32 result by an ulp)
+    # other tile widths and the other velocity-stage form change launch shapes and the grouping
+    # of some sums (FP64 wall sums, thread partitions), i.e. FP32 rounding, which the
+    # continuation amplifies up to 1e4x in the spectral coefficients: relative L2 within 1e-3
+    # (the fused-versus-oracle bound of the FP32 form, tests/test_gpu_fp32.py)
     api.set_tile_caps(p2, (2, 2, 2, 2))
+    api.set_option(p2, "velocity_split", 1 - caps[4])
     s1.step(2)
     s2.step(2)
-    for x, y in zip(_state(s1), _state(s2)):
-        assert np.allclose(x, y, rtol=0, atol=1e-6 * np.abs(y).max())
+    st1, st2 = _state(s1), _state(s2)
+    for x, y in zip(st1[:-1], st2[:-1]):
+        assert np.linalg.norm(x - y) <= 1e-3 * np.linalg.norm(y)
+    # pr (= dt p) is the small residual of an already projected field: its relative error is the
+    # velocity's divided by that residual
+    assert np.linalg.norm(st1[-1] - st2[-1]) <= 3e-2 * np.linalg.norm(st2[-1])
 
 
 def test_graph_query_and_memory():
