@@ -165,6 +165,22 @@ def cpu_baseline(steps, warmup, threads=None):
     return pts / dt / 1e6, threads, sample
 
 
+def max_over_ranks(v: float, dist=None, device="cpu") -> float:
+    """The largest v over all ranks (the job's time is its slowest replica's)."""
+    if dist is None:
+        return float(v)
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, pts, stages, seconds):
+    """Whole-job Mpts*stages/s: every replica advances its own grid of `pts` points by `stages`
+    RK stages; the job takes the slowest replica's `seconds`."""
+    return world * pts * stages / seconds / 1e6
+
+
 def run_reference(args):
     """--impl reference: the CPU restatement of the reference algorithm on the host cores."""
     rank = int(os.environ.get("RANK", "0"))
@@ -194,6 +210,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--grid", default=None, help="NX,NY,NZP: another grid of the same case (profiling, sweeps)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile widths")
+    ap.add_argument("--caps", default=None, help="Z,Y,X,FUSED,SPLIT: set these instead of autotuning")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -216,7 +233,12 @@ def main():
         cfg["nx"], cfg["ny"], cfg["nzp"] = (int(v) for v in args.grid.split(","))
     plan, s = build_solver(api, initial, cfg, api.FP32, fused=not args.refseq)
     # tile widths of each kernel family picked by timing RK steps (state restored afterwards)
-    caps = s.autotune() if not args.no_autotune else None
+    if args.caps:
+        caps = [int(v) for v in args.caps.split(",")]
+        api.set_tile_caps(plan, caps[:4])
+        api.set_option(plan, "velocity_split", caps[4])
+    else:
+        caps = s.autotune() if not args.no_autotune else None
     stream = torch.cuda.ExternalStream(plan.stream, device=torch.device("cuda", local))
     for _ in range(W):
         s.step(1)
@@ -239,12 +261,9 @@ def main():
     report = plan.profile_report()
     plan.profile(False)
     s.check()
-    t = torch.tensor([ms], device=f"cuda:{local}")
-    if dist:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms = float(t.item())
+    ms = max_over_ranks(ms, dist, f"cuda:{local}")
     pts = cfg["nx"] * cfg["ny"] * cfg["nzp"]
-    value = world * pts * cfg["ord"] * K / (ms * 1e-3) / 1e6
+    value = job_throughput(world, pts, cfg["ord"] * K, ms * 1e-3)
 
     # end to end: state uploaded from pinned host memory and downloaded every step
     fields = [f for f in (s.vx, s.vy, s.vz, s.th, s.pr)]
@@ -264,10 +283,8 @@ def main():
         api.fields_download(fields, ptrs)   # device -> pinned host, returns with the data on the host
     plan.synchronize()
     te = time.perf_counter() - t0
-    te_t = torch.tensor([te], device=f"cuda:{local}")
-    if dist:
-        dist.all_reduce(te_t, op=dist.ReduceOp.MAX)
-    e2e = world * pts * cfg["ord"] * Ke / float(te_t.item()) / 1e6
+    te = max_over_ranks(te, dist, f"cuda:{local}")
+    e2e = job_throughput(world, pts, cfg["ord"] * Ke, te)
     nbytes = sum(f.nbytes for f in fields)
 
     if rank == 0:
