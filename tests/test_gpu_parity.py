@@ -224,3 +224,15 @@ def test_fields_batched_transfer():
     api.fields_download(fields, [o.ctypes.data for o in out])
     for o, d in zip(out, data):
         assert np.array_equal(o, d)
+
+
+def test_plan_limits():
+    """Shapes the kernels cannot index (fields of 2^32 elements or more) or continue (d > 9) are
+    refused at plan creation, before any allocation."""
+    from specter_gb300 import SpecterError, api
+    with pytest.raises(SpecterError) as e:
+        api.Plan((8192, 8192, 4096 + 25), (0, 0, 25), (0, 0, 5), (1.0, 1.0, 1.0), precision=1)
+    assert e.value.code == 1
+    with pytest.raises(SpecterError) as e:
+        api.Plan((16, 16, 64), (0, 0, 25), (0, 0, 10), (1.0, 1.0, 1.0), precision=1)
+    assert e.value.code == 1
