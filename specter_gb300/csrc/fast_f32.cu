@@ -49,6 +49,9 @@ int build_fft4_table(FFT4Table &t, int n) {
         L = 2 * n - 1;
         while (!smooth235(L)) L++;
         if (!fast_pair(L, &L1, &L2)) return OK;  // no compiled four-step kernel: generic engine
+        // the Bluestein body skips the zero half of step A and the unused half of step A'
+        // (fft4.cuh), which needs n <= L/2 and an even L1
+        if (2 * n > L || L1 % 2) return OK;
         blue = 1;
     }
     int st = fast_init_device();

@@ -76,8 +76,11 @@ static inline cudaError_t fft4_ensure_tables() {
     return e;
 }
 
-// one register Stockham stage chain: a holds the data, b is scratch; result ends in `a`
-template <typename T, int N, int SIGN, int Ns>
+// one register Stockham stage chain: a holds the data, b is scratch; result ends in `a`.
+// HZ: the upper half of the input (a[i], i >= N/2) is zero and never read.  The first stage
+// (Ns = 1, no twiddles) then reads only inputs q < R/2 of each butterfly, which for radix 4 is
+// y0 = x0 + x1, y1 = x0 + s i x1, y2 = x0 - x1, y3 = x0 - s i x1; the later stages are unchanged.
+template <typename T, int N, int SIGN, int Ns, bool HZ = false>
 struct RegStages {
     static __device__ __forceinline__ void run(C2<T> *a, C2<T> *b) {
         if constexpr (Ns < N) {
@@ -85,20 +88,35 @@ struct RegStages {
             constexpr int nR = N / R;
             constexpr int step = N / (Ns * R);
             constexpr int off = reg_offset(N);
+            static_assert(!HZ || (Ns == 1 && (R == 4 || R == 2)), "half-zero input needs a first radix of 2 or 4");
 #pragma unroll
             for (int j = 0; j < nR; j++) {
                 const int k = j % Ns;
                 C2<T> t[R];
-#pragma unroll
-                for (int q = 0; q < R; q++) {
-                    t[q] = a[j + q * nR];
-                    if (q && k) {
-                        C2<T> w = regtw<T>(off + q * k * step);
-                        if (SIGN > 0) w.y = -w.y;
-                        t[q] = cmul(t[q], w);
+                if constexpr (HZ) {
+                    const C2<T> x0 = a[j];
+                    if constexpr (R == 4) {
+                        const C2<T> x1 = a[j + nR], ix1 = cmuli(x1, SIGN);
+                        t[0] = cadd(x0, x1);
+                        t[1] = cadd(x0, ix1);
+                        t[2] = csub(x0, x1);
+                        t[3] = csub(x0, ix1);
+                    } else {
+                        t[0] = x0;
+                        t[1] = x0;
                     }
+                } else {
+#pragma unroll
+                    for (int q = 0; q < R; q++) {
+                        t[q] = a[j + q * nR];
+                        if (q && k) {
+                            C2<T> w = regtw<T>(off + q * k * step);
+                            if (SIGN > 0) w.y = -w.y;
+                            t[q] = cmul(t[q], w);
+                        }
+                    }
+                    butterfly<T, R>(t, SIGN, nullptr, 0);
                 }
-                butterfly<T, R>(t, SIGN, nullptr, 0);
                 const int base = (j / Ns) * Ns * R + k;
 #pragma unroll
                 for (int q = 0; q < R; q++) b[base + q * Ns] = t[q];
@@ -115,6 +133,14 @@ __device__ __forceinline__ void dft_reg(C2<T> (&a)[N]) {
     static_assert(reg_offset(N) >= 0, "register DFT size not in the constant table");
     C2<T> b[N];
     RegStages<T, N, SIGN, 1>::run(a, b);
+}
+
+// DFT of N points whose upper half a[N/2 .. N) is zero (those entries are not read)
+template <typename T, int N, int SIGN>
+__device__ __forceinline__ void dft_reg_hz(C2<T> (&a)[N]) {
+    static_assert(reg_offset(N) >= 0 && N % 2 == 0, "register DFT size not in the constant table");
+    C2<T> b[N];
+    RegStages<T, N, SIGN, 1, true>::run(a, b);
 }
 
 // twiddle w_L^{SIGN * t} from a global table tw[t] = exp(-2 pi i t / L)
@@ -198,8 +224,13 @@ __device__ __forceinline__ int perm_pos(int k) { return L2 * (k % L1) + k / L1; 
 // Rows [n, L) are never read.  The caller fills rows [0, n) and syncs first.  The direction
 // (sign) only selects the chirp's conjugation and the filter table: the inner four-step
 // transforms are the same for both, so one body serves both directions.
+// Bluestein pads to L >= 2n - 1, so n <= L/2 = L2 * (L1/2) (L even, checked where the tables
+// are built): in step A the inputs n1 >= L1/2 are the zero padding and in step A' the outputs
+// m1 >= L1/2 are discarded, so both steps work on half of their DFT_L1 ends.
 template <typename T, int L1, int L2>
 __device__ __forceinline__ void fft4_bluestein_body(C2<T> *X, int B, const FFT4Desc &d, int sign) {
+    static_assert(L1 % 2 == 0, "Bluestein four-step needs an even L1");
+    constexpr int kH = L1 / 2;
     const int lgB = lg2(B);
     const C2<T> *tw4 = (const C2<T> *)d.tw4;
     const C2<T> *chirp = (const C2<T> *)d.chirp;
@@ -211,13 +242,15 @@ __device__ __forceinline__ void fft4_bluestein_body(C2<T> *X, int B, const FFT4D
         const int c = idx & (B - 1), n2 = idx >> lgB;
         C2<T> a[L1];
 #pragma unroll
-        for (int n1 = 0; n1 < L1; n1++) {
+        for (int n1 = 0; n1 < kH; n1++) {
             const int pos = n2 + L2 * n1;
             C2<T> w = pos < n ? __ldg(chirp + pos) : mk<T>(0, 0);
             w.y *= cs;
             a[n1] = pos < n ? cmul(X[pos * B + c], w) : mk<T>(0, 0);
         }
-        dft_reg<T, L1, -1>(a);
+#pragma unroll
+        for (int n1 = kH; n1 < L1; n1++) a[n1] = mk<T>(0, 0);  // not read by dft_reg_hz
+        dft_reg_hz<T, L1, -1>(a);
 #pragma unroll
         for (int k1 = 1; k1 < L1; k1++) a[k1] = cmul(a[k1], gtw<T, -1>(tw4, n2 * L1 + k1));
 #pragma unroll
@@ -248,7 +281,7 @@ __device__ __forceinline__ void fft4_bluestein_body(C2<T> *X, int B, const FFT4D
         for (int k1 = 0; k1 < L1; k1++) a[k1] = X[(L2 * k1 + m2) * B + c];
         dft_reg<T, L1, +1>(a);
 #pragma unroll
-        for (int m1 = 0; m1 < L1; m1++) {
+        for (int m1 = 0; m1 < kH; m1++) {
             const int pos = m2 + L2 * m1;
             if (pos < n) {
                 C2<T> w = __ldg(chirp + pos);
