@@ -12,6 +12,8 @@ constexpr int kNoFast = -1;
 // split of a working length L into L1 * L2 served by compiled four-step kernels (0 if none)
 bool fast_pair(int L, int *L1, int *L2);
 int fast_init_device();
+cudaError_t fast_x_init();  // constant tables of the x-pass unit
+cudaError_t fast_y_init();  // constant tables of the y-pass unit
 int build_fft4_table(FFT4Table &t, int n);
 void free_fft4_table(FFT4Table &t);
 

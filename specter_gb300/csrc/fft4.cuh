@@ -153,13 +153,19 @@ __device__ __forceinline__ C2<T> gtw(const C2<T> *tw, int t) {
 
 // Four-step tables of one length (FFT4Desc, plan.h), in global memory per plan:
 //   tw4[n2*L1 + k1] = w_L^{n2*k1}               (inter-step twiddles)
-//   chirp[k]        = exp(-i pi k^2 / n), k < n   (Bluestein only)
-//   filtf/filtb[k1*L2 + k2] = filter at frequency k1 + L1*k2, times 1/L (Bluestein only)
+//   chirp[k]        = exp(+i pi k^2 / n), k < n   (Bluestein only: the inverse transform's chirp)
+//   filtb[k1*L2 + k2] = FFT_L(exp(-i pi m^2 / n), m = -(n-1)..n-1) at frequency k1 + L1*k2,
+//                       times 1/L (Bluestein only)
+
+// Tile widths 8 and 16 (the usual autotuned ones) get their own instantiation of the Bluestein
+// body, so the row offsets (n*B) are compile-time immediates; other widths use the runtime form.
+constexpr int ct_lg2(int b) { return b <= 1 ? 0 : 1 + ct_lg2(b / 2); }
 
 // ---- natural -> permuted (steps A, B) ---------------------------------------------------------
-template <typename T, int L1, int L2, int SIGN>
-__device__ __forceinline__ void fft4_np(C2<T> *X, int B, const FFT4Desc &d) {
-    const int lgB = lg2(B);
+template <typename T, int L1, int L2, int SIGN, int CB>
+__device__ __forceinline__ void fft4_np_impl(C2<T> *X, int Brt, const FFT4Desc &d) {
+    const int B = CB ? CB : Brt;
+    const int lgB = CB ? ct_lg2(CB) : lg2(Brt);
     constexpr int L = L1 * L2;
     const C2<T> *tw4 = (const C2<T> *)d.tw4;
     for (int idx = threadIdx.x; idx < B * L2; idx += blockDim.x) {
@@ -187,10 +193,17 @@ __device__ __forceinline__ void fft4_np(C2<T> *X, int B, const FFT4Desc &d) {
     (void)L;
 }
 
-// ---- permuted -> natural (steps B', A') -------------------------------------------------------
+// (the x and y passes measured slower with the width-specialised copies: runtime width only)
 template <typename T, int L1, int L2, int SIGN>
-__device__ __forceinline__ void fft4_pn(C2<T> *X, int B, const FFT4Desc &d) {
-    const int lgB = lg2(B);
+__device__ __forceinline__ void fft4_np(C2<T> *X, int B, const FFT4Desc &d) {
+    fft4_np_impl<T, L1, L2, SIGN, 0>(X, B, d);
+}
+
+// ---- permuted -> natural (steps B', A') -------------------------------------------------------
+template <typename T, int L1, int L2, int SIGN, int CB>
+__device__ __forceinline__ void fft4_pn_impl(C2<T> *X, int Brt, const FFT4Desc &d) {
+    const int B = CB ? CB : Brt;
+    const int lgB = CB ? ct_lg2(CB) : lg2(Brt);
     const C2<T> *tw4 = (const C2<T> *)d.tw4;
     for (int idx = threadIdx.x; idx < B * L1; idx += blockDim.x) {
         const int c = idx & (B - 1), k1 = idx >> lgB;
@@ -216,37 +229,47 @@ __device__ __forceinline__ void fft4_pn(C2<T> *X, int B, const FFT4Desc &d) {
     __syncthreads();
 }
 
+template <typename T, int L1, int L2, int SIGN>
+__device__ __forceinline__ void fft4_pn(C2<T> *X, int B, const FFT4Desc &d) {
+    fft4_pn_impl<T, L1, L2, SIGN, 0>(X, B, d);
+}
+
 // position in the permuted layout of frequency k
 template <int L1, int L2>
 __device__ __forceinline__ int perm_pos(int k) { return L2 * (k % L1) + k / L1; }
 
 // ---- Bluestein over L = L1*L2: natural rows [0, n) in, natural rows [0, n) out -------------------
 // Rows [n, L) are never read.  The caller fills rows [0, n) and syncs first.  The direction
-// (sign) only selects the chirp's conjugation and the filter table: the inner four-step
-// transforms are the same for both, so one body serves both directions.
+// Only the inverse transform's tables are kept (chirp, filtb): the forward transform is computed
+// as conj(inverse(conj(x))), the conjugations folded into the chirp multiplies of steps A and
+// A', so one chirp and one filter table serve both directions (and one body, as the direction
+// is a runtime sign).
 // Bluestein pads to L >= 2n - 1, so n <= L/2 = L2 * (L1/2) (L even, checked where the tables
 // are built): in step A the inputs n1 >= L1/2 are the zero padding and in step A' the outputs
 // m1 >= L1/2 are discarded, so both steps work on half of their DFT_L1 ends.
-template <typename T, int L1, int L2>
-__device__ __forceinline__ void fft4_bluestein_body(C2<T> *X, int B, const FFT4Desc &d, int sign) {
+// CB: the tile width when known at compile time, else 0
+template <typename T, int L1, int L2, int CB>
+__device__ __forceinline__ void fft4_bluestein_impl(C2<T> *X, int Brt, const FFT4Desc &d, int sign) {
     static_assert(L1 % 2 == 0, "Bluestein four-step needs an even L1");
     constexpr int kH = L1 / 2;
-    const int lgB = lg2(B);
+    const int B = CB ? CB : Brt;
+    const int lgB = CB ? ct_lg2(CB) : lg2(Brt);
     const C2<T> *tw4 = (const C2<T> *)d.tw4;
     const C2<T> *chirp = (const C2<T> *)d.chirp;
-    const C2<T> *filt = (const C2<T> *)(sign < 0 ? d.filtf : d.filtb);
+    const C2<T> *filt = (const C2<T> *)d.filtb;
     const int n = d.n;
-    const T cs = sign > 0 ? (T)-1 : (T)1;  // chirp_sign = chirp or conj(chirp)
-    // step A (forward): input * chirp_sign
+    const T cs = sign < 0 ? (T)-1 : (T)1;  // forward: conjugate input and output
+    // step A (forward FFT of the convolution): conj^(sign<0)(input) * chirp
     for (int idx = threadIdx.x; idx < B * L2; idx += blockDim.x) {
         const int c = idx & (B - 1), n2 = idx >> lgB;
         C2<T> a[L1];
 #pragma unroll
         for (int n1 = 0; n1 < kH; n1++) {
             const int pos = n2 + L2 * n1;
-            C2<T> w = pos < n ? __ldg(chirp + pos) : mk<T>(0, 0);
-            w.y *= cs;
-            a[n1] = pos < n ? cmul(X[pos * B + c], w) : mk<T>(0, 0);
+            const C2<T> w = pos < n ? __ldg(chirp + pos) : mk<T>(0, 0);
+            C2<T> xv = pos < n ? X[pos * B + c] : mk<T>(0, 0);
+            xv.y *= cs;
+            a[n1] = cmul(xv, w);
         }
 #pragma unroll
         for (int n1 = kH; n1 < L1; n1++) a[n1] = mk<T>(0, 0);  // not read by dft_reg_hz
@@ -273,7 +296,7 @@ __device__ __forceinline__ void fft4_bluestein_body(C2<T> *X, int B, const FFT4D
         for (int m2 = 0; m2 < L2; m2++) X[(L2 * k1 + m2) * B + c] = b[m2];
     }
     __syncthreads();
-    // step A' (inverse), output * chirp_sign on rows < n
+    // step A' (inverse), output * chirp (conjugated for the forward transform) on rows < n
     for (int idx = threadIdx.x; idx < B * L2; idx += blockDim.x) {
         const int c = idx & (B - 1), m2 = idx >> lgB;
         C2<T> a[L1];
@@ -284,13 +307,20 @@ __device__ __forceinline__ void fft4_bluestein_body(C2<T> *X, int B, const FFT4D
         for (int m1 = 0; m1 < kH; m1++) {
             const int pos = m2 + L2 * m1;
             if (pos < n) {
-                C2<T> w = __ldg(chirp + pos);
-                w.y *= cs;
-                X[pos * B + c] = cmul(a[m1], w);
+                C2<T> o = cmul(a[m1], __ldg(chirp + pos));
+                o.y *= cs;
+                X[pos * B + c] = o;
             }
         }
     }
     __syncthreads();
+}
+
+template <typename T, int L1, int L2>
+__device__ __forceinline__ void fft4_bluestein_body(C2<T> *X, int B, const FFT4Desc &d, int sign) {
+    if (B == 8) fft4_bluestein_impl<T, L1, L2, 8>(X, 8, d, sign);
+    else if (B == 16) fft4_bluestein_impl<T, L1, L2, 16>(X, 16, d, sign);
+    else fft4_bluestein_impl<T, L1, L2, 0>(X, B, d, sign);
 }
 
 template <typename T, int L1, int L2, int SIGN>

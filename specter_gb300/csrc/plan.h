@@ -29,7 +29,7 @@ struct FFTTable {
 // length has no compiled four-step kernel and the generic engine is used
 struct FFT4Desc {
     int n, L, L1, L2, blue;
-    const void *tw4, *chirp, *filtf, *filtb;
+    const void *tw4, *chirp, *filtb;  // Bluestein: inverse chirp and filter (fft4.cuh)
 };
 struct FFT4Table {
     FFT4Desc d{};
