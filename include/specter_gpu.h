@@ -67,6 +67,10 @@ int specter_plan_create(const int n[3], const int c[3], const int o[3], const do
 int specter_plan_destroy(specter_plan *plan);            /* fcgram_destroy_plan :147-177 */
 /* info[0..7] = nx, ny, nz, Cz, oz, nx/2+1, padded kx stride, precision */
 int specter_plan_info(const specter_plan *plan, int info[8]);
+/* FFT engine per axis (x = the half length nx/2, y, z): out[4*a + 0..3] = working length L,
+ * split L1, L2 of the register four-step kernels (0, 0: the generic engine serves the axis) and
+ * 1 when the axis runs Bluestein's algorithm over L.  FP32 plans only choose four-step splits. */
+int specter_plan_engines(const specter_plan *plan, int out[12]);
 /* kx[nx/2+1], ky[ny], kz[nz], z[nz] (the kes and grid modules), dir[Cz*oz] Fortran order */
 int specter_plan_arrays(const specter_plan *plan, double *kx, double *ky, double *kz, double *z, double *dir);
 int specter_plan_synchronize(specter_plan *plan);

@@ -17,7 +17,7 @@ ERR_NAMES = {1: "SHAPE", 2: "TABLE", 3: "BC", 4: "OOM", 5: "CUDA", 6: "NONFINITE
 # every entry point declared in include/specter_gpu.h
 EXPORTS = [
     "specter_last_error", "specter_version", "specter_device_count", "specter_set_device",
-    "specter_plan_create", "specter_plan_destroy", "specter_plan_info", "specter_plan_arrays",
+    "specter_plan_create", "specter_plan_destroy", "specter_plan_info", "specter_plan_engines", "specter_plan_arrays",
     "specter_plan_synchronize", "specter_plan_stream",
     "specter_field_create", "specter_field_destroy", "specter_field_upload", "specter_field_download",
     "specter_field_copy", "specter_field_zero", "specter_field_device_ptr",

@@ -49,6 +49,11 @@ class Plan:
         check(L.specter_plan_info(h, info))
         self.nx, self.ny, self.nz, self.cz, self.oz, self.nxh, self.ldx, self.precision = list(info)
         self.nzp = self.nz - self.cz
+        eng = (C.c_int * 12)()
+        check(L.specter_plan_engines(h, eng))
+        # per axis: working length, four-step split (L1, L2; 0 = generic engine), Bluestein flag
+        self.engines = {ax: dict(L=eng[4 * i], L1=eng[4 * i + 1], L2=eng[4 * i + 2], bluestein=bool(eng[4 * i + 3]))
+                        for i, ax in enumerate("xyz")}
         self.lengths = tuple(lengths)
         self.rdtype = np.float64 if self.precision == FP64 else np.float32
         self.cdtype = np.complex128 if self.precision == FP64 else np.complex64

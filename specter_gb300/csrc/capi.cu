@@ -130,6 +130,22 @@ int specter_plan_info(const specter_plan *plan, int info[8]) {
     return SPECTER_OK;
 }
 
+int specter_plan_engines(const specter_plan *plan, int out[12]) {
+    CHECK_PLAN(plan);
+    if (!out) { set_error("null argument"); return SPECTER_ERR_ARG; }
+    const Plan &P = *plan->p;
+    const FFTTable *gen[3] = {&P.tx, &P.ty, &P.tz};
+    const FFT4Table *four[3] = {&P.tx4, &P.ty4, &P.tz4};
+    for (int a = 0; a < 3; a++) {
+        const bool f = four[a]->ok;
+        out[4 * a + 0] = f ? four[a]->d.L : gen[a]->d.L;
+        out[4 * a + 1] = f ? four[a]->d.L1 : 0;
+        out[4 * a + 2] = f ? four[a]->d.L2 : 0;
+        out[4 * a + 3] = f ? four[a]->d.blue : gen[a]->d.blue;
+    }
+    return SPECTER_OK;
+}
+
 int specter_plan_arrays(const specter_plan *plan, double *kx, double *ky, double *kz, double *z, double *dir) {
     CHECK_PLAN(plan);
     const Plan &P = *plan->p;

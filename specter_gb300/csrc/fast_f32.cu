@@ -10,17 +10,13 @@
 
 namespace sg {
 
-// Compiled splits L = L1 * L2: z (Bluestein lengths of nz = 538 and 282), y (512, 256) and
-// x (H = 256, 128) of the 512^3- and 256^3-class grids.
-bool fast_pair(int L, int *L1, int *L2) {
-    switch (L) {
-    case 1080: *L1 = 36; *L2 = 30; return true;
-    case 576: *L1 = 24; *L2 = 24; return true;
-    case 512: *L1 = 32; *L2 = 16; return true;
-    case 256: *L1 = 16; *L2 = 16; return true;
-    case 128: *L1 = 16; *L2 = 8; return true;
-    default: return false;
-    }
+bool fast_pair(int axis, int L, int *L1, int *L2) {
+#define SG_PAIR_CASE(A, B) if (L == (A) * (B)) { *L1 = A; *L2 = B; return true; }
+    if (axis == kFastZ) { SG_FAST_PAIRS_Z(SG_PAIR_CASE) }
+    if (axis == kFastY) { SG_FAST_PAIRS_Y(SG_PAIR_CASE) }
+    if (axis == kFastX) { SG_FAST_PAIRS_X(SG_PAIR_CASE) }
+#undef SG_PAIR_CASE
+    return false;
 }
 
 static bool smooth235(int m) {
@@ -47,16 +43,19 @@ int fast_init_device() {
     return OK;
 }
 
-int build_fft4_table(FFT4Table &t, int n) {
+// Tables of the four-step engine for an axis of length n: the length itself when it has a
+// compiled split, else (z only) Bluestein over the smallest compiled length L >= 2n - 1.  The
+// Bluestein body skips the zero half of step A and the unused half of step A' (fft4.cuh), which
+// needs n <= L/2 and an even L1.  No table (t.ok = 0): the generic engine serves the axis.
+int build_fft4_table(FFT4Table &t, int n, int axis) {
     t = FFT4Table{};
     int L1 = 0, L2 = 0, L = n, blue = 0;
-    if (!fast_pair(n, &L1, &L2)) {
-        L = 2 * n - 1;
-        while (!smooth235(L)) L++;
-        if (!fast_pair(L, &L1, &L2)) return OK;  // no compiled four-step kernel: generic engine
-        // the Bluestein body skips the zero half of step A and the unused half of step A'
-        // (fft4.cuh), which needs n <= L/2 and an even L1
-        if (2 * n > L || L1 % 2) return OK;
+    if (!fast_pair(axis, n, &L1, &L2)) {
+        if (axis != kFastZ) return OK;
+        L = 0;
+        for (int m = 2 * n - 1; m <= 4 * n && !L; m++)
+            if (smooth235(m) && 2 * n <= m && fast_pair(axis, m, &L1, &L2) && L1 % 2 == 0) L = m;
+        if (!L) return OK;
         blue = 1;
     }
     int st = fast_init_device();
@@ -110,10 +109,10 @@ void free_fft4_table(FFT4Table &t) {
 }
 
 int fast_z_inverse(Plan &P, const ZInvArgs &a, int nf, double bytes) {
-    return dispatch(P, P.tz4, [&](auto l1, auto l2) { return zinv<decltype(l1)::value, decltype(l2)::value>(P, a, nf, bytes); });
+    return dispatch_z(P, P.tz4, [&](auto l1, auto l2) { return zinv<decltype(l1)::value, decltype(l2)::value>(P, a, nf, bytes); });
 }
 int fast_z_forward(Plan &P, const ZFwdArgs &a, int nf, double bytes) {
-    return dispatch(P, P.tz4, [&](auto l1, auto l2) { return zfwd<decltype(l1)::value, decltype(l2)::value>(P, a, nf, bytes); });
+    return dispatch_z(P, P.tz4, [&](auto l1, auto l2) { return zfwd<decltype(l1)::value, decltype(l2)::value>(P, a, nf, bytes); });
 }
 
 }  // namespace sg

@@ -121,18 +121,18 @@ int xnl(Plan &P, const XNLArgs &a, double bytes) {
 
 template <int V> using IC = std::integral_constant<int, V>;
 
-// calls fn(IC<L1>, IC<L2>) for the compiled split of the table's length
-template <typename Fn>
-static int dispatch(const Plan &P, const FFT4Table &t, Fn &&fn) {
-    if (P.prec != FP32 || !t.ok) return kNoFast;
-    const int l1 = t.d.L1, l2 = t.d.L2;
-    if (l1 == 36 && l2 == 30) return fn(IC<36>{}, IC<30>{});
-    if (l1 == 24 && l2 == 24) return fn(IC<24>{}, IC<24>{});
-    if (l1 == 32 && l2 == 16) return fn(IC<32>{}, IC<16>{});
-    if (l1 == 16 && l2 == 16) return fn(IC<16>{}, IC<16>{});
-    if (l1 == 16 && l2 == 8) return fn(IC<16>{}, IC<8>{});
-    return kNoFast;
-}
-
+// calls fn(IC<L1>, IC<L2>) for the compiled split of the table's length on that axis
+#define SG_DISPATCH_CASE(A, B) if (l1 == (A) && l2 == (B)) return fn(IC<A>{}, IC<B>{});
+#define SG_DEFINE_DISPATCH(NAME, LIST)                                      \
+    template <typename Fn>                                                  \
+    static int NAME(const Plan &P, const FFT4Table &t, Fn &&fn) {           \
+        if (P.prec != FP32 || !t.ok) return kNoFast;                        \
+        const int l1 = t.d.L1, l2 = t.d.L2;                                 \
+        LIST(SG_DISPATCH_CASE)                                              \
+        return kNoFast;                                                     \
+    }
+SG_DEFINE_DISPATCH(dispatch_x, SG_FAST_PAIRS_X)
+SG_DEFINE_DISPATCH(dispatch_y, SG_FAST_PAIRS_Y)
+SG_DEFINE_DISPATCH(dispatch_z, SG_FAST_PAIRS_Z)
 
 }  // namespace sg

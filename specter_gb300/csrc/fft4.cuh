@@ -22,7 +22,7 @@
 namespace sg {
 
 // ---- register DFT sizes served by the constant twiddle table -------------------------------
-constexpr int kRegSizes[] = {8, 9, 10, 12, 15, 16, 18, 20, 24, 27, 30, 32, 36, 40, 45, 48, 64};
+constexpr int kRegSizes[] = {4, 6, 8, 9, 10, 12, 15, 16, 18, 20, 24, 27, 30, 32, 36, 40, 45, 48, 64};
 constexpr int kNumRegSizes = sizeof(kRegSizes) / sizeof(int);
 constexpr int reg_offset(int N) {
     int off = 0;

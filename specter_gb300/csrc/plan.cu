@@ -269,8 +269,8 @@ int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], cons
         plan_destroy(p);
         return st;
     }
-    if (p->prec == FP32 && ((st = build_fft4_table(p->tx4, p->H)) || (st = build_fft4_table(p->ty4, ny)) ||
-                            (st = build_fft4_table(p->tz4, nz)))) {
+    if (p->prec == FP32 && ((st = build_fft4_table(p->tx4, p->H, 0)) || (st = build_fft4_table(p->ty4, ny, 1)) ||
+                            (st = build_fft4_table(p->tz4, nz, 2)))) {
         plan_destroy(p);
         return st;
     }

@@ -127,7 +127,7 @@ unsigned long long plan_bytes(const Plan &P);
 int table_check(const char *tdir, int C, int d, double out[3]);
 int build_fft_table(FFTTable &t, int n, Prec prec);
 void free_fft_table(FFTTable &t);
-int build_fft4_table(FFT4Table &t, int n);  // fast_f32.cu
+int build_fft4_table(FFT4Table &t, int n, int axis);  // fast_f32.cu; axis 0 = x, 1 = y, 2 = z
 void free_fft4_table(FFT4Table &t);
 
 }  // namespace sg

@@ -54,7 +54,7 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a))
 
 
-def run(instances=64, steps=200, seed=20261203, seq_sample=None, autotune=True):
+def run(instances=64, steps=200, seed=20261203, seq_sample=None, autotune=True, graph_steps=1):
     from specter_gb300 import api, initial
     insts = draw(instances, seed)
     t0 = time.perf_counter()
@@ -66,11 +66,13 @@ def run(instances=64, steps=200, seed=20261203, seq_sample=None, autotune=True):
         caps.append(s.autotune() if autotune else None)
     t_tune = time.perf_counter() - t0
     solvers = [s for _, s in built]
-    graph = api.Graph(solvers, nsteps=1)
+    if steps % graph_steps:
+        raise ValueError("steps must be a multiple of graph_steps")
+    graph = api.Graph(solvers, nsteps=graph_steps)
     for p, _ in built:
         p.synchronize()
     t0 = time.perf_counter()
-    for _ in range(steps):
+    for _ in range(steps // graph_steps):
         graph.launch()
     graph.synchronize()
     t_run = time.perf_counter() - t0
@@ -79,7 +81,8 @@ def run(instances=64, steps=200, seed=20261203, seq_sample=None, autotune=True):
     solves_per_s = instances / t_run
     pts = sum(x["nx"] * x["ny"] * x["nzp"] * x["ord"] for x in insts) * steps
     result = {"instances": instances, "steps": steps, "seed": seed, "precision": "fp32-bulk",
-              "graph_kernels_per_step": graph.kernels, "seconds": round(t_run, 4),
+              "graph_steps": graph_steps, "graph_kernels_per_step": graph.kernels // graph_steps,
+              "seconds": round(t_run, 4),
               "solves_per_s": round(solves_per_s, 3), "mpts_stages_per_s": round(pts / t_run / 1e6, 2),
               "build_s": round(t_build, 2), "autotune_s": round(t_tune, 2), "caps": caps}
     # sequential plain FP64 on a sample (first k instances): time per solve, error of the ensemble
@@ -126,8 +129,9 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--seq-sample", type=int, default=None, help="instances run through sequential FP64")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--graph-steps", type=int, default=1, help="RK steps captured per graph launch")
     args = ap.parse_args(argv)
-    res, _, _ = run(args.instances, args.steps, args.seed, args.seq_sample, not args.no_autotune)
+    res, _, _ = run(args.instances, args.steps, args.seed, args.seq_sample, not args.no_autotune, args.graph_steps)
     print(json.dumps(res), flush=True)
     return res
 

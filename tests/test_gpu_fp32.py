@@ -1,6 +1,8 @@
 """FP32-bulk (precision form) kernels against the FP64 oracle on grids that select the
 register four-step FFT kernels: 256 x 256 x 257 (+25) -> y 256 = 16*16, x H = 128 = 16*8,
-z Bluestein 576 = 24*24; 128 x 128 x 513 (+25) -> z Bluestein 1080 = 36*30.
+z Bluestein 576 = 24*24; 128 x 128 x 513 (+25) -> z Bluestein 1080 = 36*30; and the small
+grids of the ensemble and the served stream: z 90 = 10*9 directly, Bluestein 128 = 16*8 (nz 58),
+256 = 16*16 (nz 122), 320 = 20*16 (nz 154); x H = 16 ... 64 and y 32 ... 128 (SPLITS below).
 
 FP32 rounding of the d wall-adjacent points is amplified by the continuation (sum |dir| = 9.5e3):
 rounding a smooth column to FP32 alone (2.5e-8) already gives ~2e-5 relative error in its
@@ -26,10 +28,32 @@ def smooth_real(g, rng, nmodes=6, kmax=4):
     return r
 
 
-@pytest.fixture(scope="module", params=[(256, 256, 257, 2.0), (128, 128, 513, 1.0)], ids=["256", "128x513"])
+# grid -> expected engine per axis: (L, L1, L2, Bluestein)
+SPLITS = {
+    (256, 256, 257): {"x": (128, 16, 8, False), "y": (256, 16, 16, False), "z": (576, 24, 24, True)},
+    (128, 128, 513): {"x": (64, 8, 8, False), "y": (128, 16, 8, False), "z": (1080, 36, 30, True)},
+    (48, 96, 65): {"x": (24, 6, 4, False), "y": (96, 12, 8, False), "z": (90, 10, 9, False)},
+    (32, 64, 33): {"x": (16, 4, 4, False), "y": (64, 8, 8, False), "z": (128, 16, 8, True)},
+    (64, 48, 97): {"x": (32, 8, 4, False), "y": (48, 8, 6, False), "z": (256, 16, 16, True)},
+    (96, 32, 129): {"x": (48, 8, 6, False), "y": (32, 8, 4, False), "z": (320, 20, 16, True)},
+}
+GRIDS = [(256, 256, 257, 2.0), (128, 128, 513, 1.0), (48, 96, 65, 2.0), (32, 64, 33, 2.0), (64, 48, 97, 2.0),
+         (96, 32, 129, 2.0)]
+
+
+@pytest.fixture(scope="module", params=GRIDS, ids=["256", "128x513", "48x96x65", "32x64x33", "64x48x97", "96x32x129"])
 def pair32(request):
     nx, ny, nzp, Lz = request.param
     return make_pair(nx, ny, nzp, Lz, precision=1)
+
+
+def test_engine_splits(pair32):
+    """Each grid runs the four-step split it is meant to exercise (not the generic engine)."""
+    plan, g = pair32
+    want = SPLITS[(plan.nx, plan.ny, plan.nzp)]
+    for ax in "xyz":
+        e = plan.engines[ax]
+        assert (e["L"], e["L1"], e["L2"], e["bluestein"]) == want[ax], (ax, e)
 
 
 def test_transforms_fp32(pair32):
