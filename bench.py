@@ -118,6 +118,42 @@ def dominant_roofline(report, hbm_peak, traffic_table):
             "launches": n, "share": round(ms / sum(v[1] for v in report.values()), 4)}
 
 
+def fft_flops_per_stage(cfg, z_engine):
+    """Model FFT operation count of one fused BOUSS RK stage (the secondary figure): 5 L log2 L
+    per complex length-L transform, Bluestein counted at its padded length L (two length-L
+    transforms plus the chirp and filter multiplies), 2.5 nx log2 nx per real x transform.
+    Transforms per column, counted from the kernels: z 23 = z_inverse 4 fields x (value, d/dz)
+    + fused_vcomp 3 x (NL forward, round trip inverse + forward) + fused_vproj 1 (pressure)
+    + fused_theta 5; y 16 = 12 inverse (value, d/dy, d/dz of 4 fields) + 4 forward (NL);
+    x 19 = 15 c2r + 4 r2c (x_nonlinear)."""
+    import math
+    nx, ny, nzp = cfg["nx"], cfg["ny"], cfg["nzp"]
+    nz, nxh = nzp + cfg["cz"], cfg["nx"] // 2 + 1
+
+    def cfft(L):
+        return 5.0 * L * math.log2(L)
+    L = z_engine["L"]
+    z_col = 2 * cfft(L) + 6.0 * (2 * nz + L) if z_engine["bluestein"] else cfft(nz)
+    return 23 * nxh * ny * z_col + 16 * nxh * nzp * cfft(ny) + 19 * ny * nzp * 2.5 * nx * math.log2(nx)
+
+
+def fp64_gemm_tflops(device):
+    """Measured FP64 peak: torch.matmul (cuBLAS DGEMM) of 8192^3, best of 3."""
+    import torch
+    a = torch.randn(8192, 8192, dtype=torch.float64, device=device)
+    b = torch.randn(8192, 8192, dtype=torch.float64, device=device)
+    torch.matmul(a, b)
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) * 1e-3)
+    return 2.0 * 8192 ** 3 / best / 1e12
+
+
 def load_traffic():
     """Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of each kernel from
     the committed ncu summary of this workload: the rows '| kernel | launches | bytes per launch |'
@@ -211,6 +247,8 @@ def main():
     ap.add_argument("--grid", default=None, help="NX,NY,NZP: another grid of the same case (profiling, sweeps)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile widths")
     ap.add_argument("--caps", default=None, help="Z,Y,X,FUSED,SPLIT: set these instead of autotuning")
+    ap.add_argument("--fp64", action="store_true",
+                    help="the plain FP64 form instead of FP32-bulk (not the headline: reported against the FP64 peak)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -231,9 +269,11 @@ def main():
     cfg = dict(CFG)
     if args.grid:
         cfg["nx"], cfg["ny"], cfg["nzp"] = (int(v) for v in args.grid.split(","))
-    plan, s = build_solver(api, initial, cfg, api.FP32, fused=not args.refseq)
+    plan, s = build_solver(api, initial, cfg, api.FP64 if args.fp64 else api.FP32, fused=not args.refseq)
     # tile widths of each kernel family picked by timing RK steps (state restored afterwards)
-    if args.caps:
+    if args.fp64:
+        caps = None
+    elif args.caps:
         caps = [int(v) for v in args.caps.split(",")]
         api.set_tile_caps(plan, caps[:4])
         api.set_option(plan, "velocity_split", caps[4])
@@ -294,27 +334,39 @@ def main():
         roof["peak_kind"] = peak_kind
         # stage-level model of the frozen measurement definition: B = 128 * N * s per BOUSS stage
         N = cfg["nx"] * cfg["ny"] * (cfg["nzp"] + cfg["cz"])
-        model_gbs = 128 * N * 4 * cfg["ord"] * K / (ms * 1e-3) / 1e9
+        es = 8 if args.fp64 else 4
+        model_gbs = 128 * N * es * cfg["ord"] * K / (ms * 1e-3) / 1e9
+        # secondary figure: model FFT flops per second against the FP32 CUDA-core FMA rate at the
+        # maximum SM clock (152 SMs x 128 lanes x 2), or against measured DGEMM for the FP64 form
+        flops = fft_flops_per_stage(cfg, plan.engines["z"]) * cfg["ord"] * K / (ms * 1e-3) / 1e12
+        if args.fp64:
+            fpeak, fkind = fp64_gemm_tflops(f"cuda:{local}"), "measured FP64 DGEMM (torch.matmul 8192^3)"
+        else:
+            fpeak, fkind = 152 * 128 * 2 * 2.07e9 / 1e12, "nominal FP32 FMA rate at 2070 MHz"
         line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": K,
                 "warmup": W, "ms_per_step": round(ms / K, 4), "higher_is_better": True,
-                "scaling": "weak" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32",
+                "scaling": "weak" if world > 1 else "weak", "vs_baseline": None, "dtype": "f64" if args.fp64 else "f32",
                 "data": "synthetic",
                 "config": {"workload": f"BOUSS Rayleigh-Benard {cfg['nx']}x{cfg['ny']}x{cfg['nzp']} (+{cfg['cz']} FC-Gram, "
-                                       f"NZ={cfg['nzp'] + cfg['cz']}), FP32-bulk, RK2, dt=1e-5",
+                                       f"NZ={cfg['nzp'] + cfg['cz']}), {'plain FP64' if args.fp64 else 'FP32-bulk'}, "
+                                       f"RK2, dt=1e-5",
                            "path": "reference-sequence" if args.refseq else "fused",
                            "autotune_caps_z_y_x_fused_split": list(caps) if caps else None,
                            "l2": f"inputs larger than L2 ({field_mb:.0f} MB per field), no flush",
                            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
                 "roofline": roof,
-                "stage_model": {"bytes_per_stage": 128 * N * 4, "achieved_gbs": round(model_gbs, 1),
+                "stage_model": {"bytes_per_stage": 128 * N * es, "achieved_gbs": round(model_gbs, 1),
                                 "frac": round(model_gbs / peak, 4)},
+                "fft_flops": {"per_stage": round(fft_flops_per_stage(cfg, plan.engines["z"])),
+                              "achieved_tflops": round(flops, 2), "peak_tflops": round(fpeak, 1),
+                              "peak_kind": fkind, "frac": round(flops / fpeak, 4)},
                 "kernels": {k: {"launches": v[0], "ms": round(v[1], 3),
                                 "gbs": round(v[2] / (v[1] * 1e-3) / 1e9, 1) if v[1] > 0 else None}
                             for k, v in sorted(report.items(), key=lambda kv: -kv[1][1])},
                 "clocks": clocks.summary(),
                 "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes},
                 "gpu_launches": launches}
-        if not args.no_cpu and world == 1:
+        if not args.no_cpu and not args.fp64 and world == 1:
             v, cores, sample = cpu_baseline(1, 0)
             line["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
         print(json.dumps(line), flush=True)
