@@ -83,32 +83,23 @@ int ypass(Plan &P, const YArgs &a0, int nf, int nplanes, double bytes) {
     return done("y_pass");
 }
 
-// x lengths whose passes switch to the lane-pair engine when a step has at most half a block
-// of items (2 * rows * max(L1, L2) <= threads): H = 256 and 128 (nx = 512, 256)
-template <int L1, int L2> constexpr bool kXPair = (L1 == 16 && (L2 == 16 || L2 == 8));
-template <int L1, int L2> bool x_pair(int rb) { return kXPair<L1, L2> && 2 * rb * (L1 > L2 ? L1 : L2) <= kThreads; }
-
 template <int L1, int L2>
 int xpass(Plan &P, const XArgs &a, int nf, bool r2c, double bytes) {
     using E = FourStep<float, L1, L2>;
-    using EP = std::conditional_t<kXPair<L1, L2>, FourStepPair<float, L1, L2>, E>;
     int rb = 0;
     for (int t : {16, 8, 4, 2, 1})
         if (t <= P.tile_cap[Plan::kTileX] && x_pass_elems<E>(P.tx4.d, P.nxh, t) * sizeof(float2) <= kFastBudget) { rb = t; break; }
     if (!rb) return kNoFast;
     const size_t sm = x_pass_elems<E>(P.tx4.d, P.nxh, rb) * sizeof(float2);
     const dim3 grid(cdiv(a.nrows * P.ny, rb), 1, nf);
-    const bool pr = x_pair<L1, L2>(rb);
     if (r2c) {
-        auto k = pr ? k_x_r2c<float, EP> : k_x_r2c<float, E>;
-        smem_attr(k, sm);
+        smem_attr(k_x_r2c<float, E>, sm);
         Scope s(P, "x_r2c", bytes);
-        k<<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a.prepared(), rb);
+        k_x_r2c<float, E><<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a.prepared(), rb);
     } else {
-        auto k = pr ? k_x_c2r<float, EP> : k_x_c2r<float, E>;
-        smem_attr(k, sm);
+        smem_attr(k_x_c2r<float, E>, sm);
         Scope s(P, "x_c2r", bytes);
-        k<<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a.prepared(), rb);
+        k_x_c2r<float, E><<<grid, kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a.prepared(), rb);
     }
     return done(r2c ? "x_r2c" : "x_c2r");
 }
@@ -116,16 +107,14 @@ int xpass(Plan &P, const XArgs &a, int nf, bool r2c, double bytes) {
 template <int L1, int L2>
 int xnl(Plan &P, const XNLArgs &a, double bytes) {
     using E = FourStep<float, L1, L2>;
-    using EP = std::conditional_t<kXPair<L1, L2>, FourStepPair<float, L1, L2>, E>;
     int rb = 0;
     for (int t : {16, 8, 4, 2, 1})
         if (t <= P.tile_cap[Plan::kTileX] && x_nl_elems<E>(P.tx4.d, P.nxh, P.H, t) * sizeof(float2) <= kMaxSmem) { rb = t; break; }
     if (!rb) return kNoFast;
     const size_t sm = x_nl_elems<E>(P.tx4.d, P.nxh, P.H, rb) * sizeof(float2);
-    auto k = x_pair<L1, L2>(rb) ? k_x_nonlinear<float, EP> : k_x_nonlinear<float, E>;
-    smem_attr(k, sm);
+    smem_attr(k_x_nonlinear<float, E>, sm);
     Scope s(P, "x_nonlinear", bytes);
-    k<<<dim3(cdiv(a.nrows * P.ny, rb)), kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a.prepared(), rb);
+    k_x_nonlinear<float, E><<<dim3(cdiv(a.nrows * P.ny, rb)), kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a.prepared(), rb);
     return done("x_nonlinear");
 }
 }  // namespace

@@ -234,120 +234,6 @@ __device__ __forceinline__ void fft4_pn(C2<T> *X, int B, const FFT4Desc &d) {
     fft4_pn_impl<T, L1, L2, SIGN, 0>(X, B, d);
 }
 
-// ---- lane-pair variant (tiles too narrow to give every thread an item) ---------------------------
-// With B * L2 and B * L1 at most half the block (the x passes at 8 rows: 128 items for 256
-// threads) each item is shared by two adjacent lanes: lane h of the pair holds the points of
-// parity h, transforms them (DFT_{N/2}), lane 1 applies w_N^j, the pair swaps its halves with one
-// shuffle per value and lane h keeps outputs h*N/2 + j.  Same layouts, twiddles and permuted
-// output as fft4_np / fft4_pn; about a third more instructions per item but half the work on
-// each lane's dependency chain, and all lanes busy.  The loop runs whole warps (idle lanes redo
-// the warp's first item and store nothing) because the shuffles need every lane.
-
-// in: a[j] = x[2j + h], j < N/2; out: a[j] = X[h*N/2 + j]
-template <typename T, int N, int SIGN>
-__device__ __forceinline__ void dft_pair(C2<T> (&a)[N / 2], int h) {
-    constexpr int M = N / 2;
-    constexpr int off = reg_offset(N);
-    static_assert(N % 2 == 0 && reg_offset(N) >= 0 && reg_offset(M) >= 0, "pair DFT sizes");
-    dft_reg<T, M, SIGN>(a);  // E (lane 0) or O (lane 1)
-#pragma unroll
-    for (int j = 1; j < M; j++) {
-        C2<T> w = regtw<T>(off + j);
-        if (SIGN > 0) w.y = -w.y;
-        const C2<T> one = mk<T>(1, 0);
-        a[j] = cmul(a[j], h ? w : one);  // lane 1: w_N^j O_j
-    }
-    const T sg = h ? (T)-1 : (T)1;
-#pragma unroll
-    for (int j = 0; j < M; j++) {
-        C2<T> o;
-        o.x = __shfl_xor_sync(0xffffffffu, a[j].x, 1);
-        o.y = __shfl_xor_sync(0xffffffffu, a[j].y, 1);
-        // lane 0: E_j + wO_j; lane 1: E_j - wO_j = o - a
-        a[j] = mk<T>(o.x + sg * a[j].x, o.y + sg * a[j].y);
-    }
-}
-
-template <typename T, int L1, int L2, int SIGN>
-__device__ __forceinline__ void fft4_np_pair(C2<T> *X, int B, const FFT4Desc &d) {
-    constexpr int H1 = L1 / 2, H2 = L2 / 2;
-    const int lgB = lg2(B), lane = threadIdx.x & 31, h = threadIdx.x & 1;
-    const C2<T> *tw4 = (const C2<T> *)d.tw4;
-    for (int base = threadIdx.x - lane; base < 2 * B * L2; base += blockDim.x) {
-        const int idx = base + lane;
-        const bool act = idx < 2 * B * L2;
-        const int it = (act ? idx : base + h) >> 1, c = it & (B - 1), n2 = it >> lgB;
-        C2<T> a[H1];
-#pragma unroll
-        for (int j = 0; j < H1; j++) a[j] = X[(n2 + L2 * (2 * j + h)) * B + c];
-        dft_pair<T, L1, SIGN>(a, h);
-#pragma unroll
-        for (int j = 0; j < H1; j++) {
-            const int k1 = h * H1 + j;
-            if (k1) a[j] = cmul(a[j], gtw<T, SIGN>(tw4, n2 * L1 + k1));
-        }
-        if (act) {
-#pragma unroll
-            for (int j = 0; j < H1; j++) X[(n2 + L2 * (h * H1 + j)) * B + c] = a[j];
-        }
-    }
-    __syncthreads();
-    for (int base = threadIdx.x - lane; base < 2 * B * L1; base += blockDim.x) {
-        const int idx = base + lane;
-        const bool act = idx < 2 * B * L1;
-        const int it = (act ? idx : base + h) >> 1, c = it & (B - 1), k1 = it >> lgB;
-        C2<T> b[H2];
-#pragma unroll
-        for (int j = 0; j < H2; j++) b[j] = X[(L2 * k1 + 2 * j + h) * B + c];
-        dft_pair<T, L2, SIGN>(b, h);
-        if (act) {
-#pragma unroll
-            for (int j = 0; j < H2; j++) X[(L2 * k1 + h * H2 + j) * B + c] = b[j];
-        }
-    }
-    __syncthreads();
-}
-
-template <typename T, int L1, int L2, int SIGN>
-__device__ __forceinline__ void fft4_pn_pair(C2<T> *X, int B, const FFT4Desc &d) {
-    constexpr int H1 = L1 / 2, H2 = L2 / 2;
-    const int lgB = lg2(B), lane = threadIdx.x & 31, h = threadIdx.x & 1;
-    const C2<T> *tw4 = (const C2<T> *)d.tw4;
-    for (int base = threadIdx.x - lane; base < 2 * B * L1; base += blockDim.x) {
-        const int idx = base + lane;
-        const bool act = idx < 2 * B * L1;
-        const int it = (act ? idx : base + h) >> 1, c = it & (B - 1), k1 = it >> lgB;
-        C2<T> b[H2];
-#pragma unroll
-        for (int j = 0; j < H2; j++) b[j] = X[(L2 * k1 + 2 * j + h) * B + c];
-        dft_pair<T, L2, SIGN>(b, h);
-#pragma unroll
-        for (int j = 0; j < H2; j++) {
-            const int m2 = h * H2 + j;
-            if (m2) b[j] = cmul(b[j], gtw<T, SIGN>(tw4, m2 * L1 + k1));
-        }
-        if (act) {
-#pragma unroll
-            for (int j = 0; j < H2; j++) X[(L2 * k1 + h * H2 + j) * B + c] = b[j];
-        }
-    }
-    __syncthreads();
-    for (int base = threadIdx.x - lane; base < 2 * B * L2; base += blockDim.x) {
-        const int idx = base + lane;
-        const bool act = idx < 2 * B * L2;
-        const int it = (act ? idx : base + h) >> 1, c = it & (B - 1), m2 = it >> lgB;
-        C2<T> a[H1];
-#pragma unroll
-        for (int j = 0; j < H1; j++) a[j] = X[(L2 * (2 * j + h) + m2) * B + c];
-        dft_pair<T, L1, SIGN>(a, h);
-        if (act) {
-#pragma unroll
-            for (int j = 0; j < H1; j++) X[(m2 + L2 * (h * H1 + j)) * B + c] = a[j];
-        }
-    }
-    __syncthreads();
-}
-
 // position in the permuted layout of frequency k
 template <int L1, int L2>
 __device__ __forceinline__ int perm_pos(int k) { return L2 * (k % L1) + k / L1; }

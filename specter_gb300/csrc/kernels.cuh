@@ -98,26 +98,6 @@ struct FourStep {
     static __device__ __forceinline__ int pos(int k, const Desc &d) { return d.blue ? k : perm_pos<L1, L2>(k); }
 };
 
-// FourStep whose plain (non-Bluestein) transforms share each item between two lanes
-// (fft4_np_pair / fft4_pn_pair): for tiles with at most half a block of items per step, as in
-// the x passes at 8 rows (H = 256 or 128).  Same layouts and permuted order as FourStep.
-template <typename T, int L1, int L2>
-struct FourStepPair : FourStep<T, L1, L2, false> {
-    using Base = FourStep<T, L1, L2, false>;
-    static __device__ __forceinline__ C2<T> *run(C2<T> *X, C2<T> *Y, int B, const FFT4Desc &d, int sign) {
-        if (d.blue) return Base::run(X, Y, B, d, sign);
-        if (sign < 0) fft4_np_pair<T, L1, L2, -1>(X, B, d);
-        else fft4_np_pair<T, L1, L2, +1>(X, B, d);
-        return X;
-    }
-    static __device__ __forceinline__ C2<T> *run_perm(C2<T> *X, C2<T> *Y, int B, const FFT4Desc &d, int sign) {
-        if (d.blue) return Base::run(X, Y, B, d, sign);
-        if (sign < 0) fft4_pn_pair<T, L1, L2, -1>(X, B, d);
-        else fft4_pn_pair<T, L1, L2, +1>(X, B, d);
-        return X;
-    }
-};
-
 // ---------------------------------------------------------------------------------
 // z pass, inverse: out0 = scale * IFFT_z(in) (+ add), out1 = scale * IFFT_z(i kz in).
 // Rows [0, nrows) are written.  fftp1d_complex_to_real_z, src/fftp/fftp.fpp:1060-1094.

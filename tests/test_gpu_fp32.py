@@ -131,36 +131,3 @@ def test_stage_fp32(pair32, solver):
     cons = [rel(a, b) for a, b in zip(outs[True], outs[False])]
     print("fused vs reference sequence", ["%.2e" % e for e in cons])
     assert max(cons) < 1e-3
-
-
-@pytest.mark.parametrize("shape", [(256, 32, 33), (512, 16, 33)], ids=["H128", "H256"])
-def test_x_lane_pair_engine(shape):
-    """At 8 rows per block the x passes of H = 128 and 256 share each FFT item between two lanes
-    (FourStepPair); at 16 rows they use one lane per item.  Both against the oracle (transforms
-    and the nonlinear pass), and against each other."""
-    from specter_gb300 import api
-    nx, ny, nzp = shape
-    plan, g = make_pair(nx, ny, nzp, 2.0, precision=1)
-    rng = np.random.default_rng(15)
-    r = smooth_real(g, rng)
-    ref_r2c = g.fftp3d_real_to_complex(r)
-    ref_c2r = g.fftp3d_complex_to_real(ref_r2c)
-    v = [smooth_spectral(g, rng) for _ in range(3)]
-    ref_nl = g.gradre(*v)
-    got = {}
-    for cap in (8, 16):
-        api.set_tile_caps(plan, [16, 16, cap, 16])
-        out = plan.field()
-        api.fftp3d_real_to_complex(plan, plan.field(1, data=r), out)
-        rout = plan.field(1)
-        api.fftp3d_complex_to_real(plan, plan.field(data=ref_r2c), rout)
-        nl = [plan.field() for _ in range(3)]
-        api.gradre(plan, *[plan.field(data=x) for x in v], *nl)
-        got[cap] = [out.download(), rout.download()] + [f.download() for f in nl]
-        errs = [rel(got[cap][0], ref_r2c), rel(got[cap][1], ref_c2r)] + [rel(a, b) for a, b in zip(got[cap][2:], ref_nl)]
-        print(cap, ["%.2e" % e for e in errs])
-        assert errs[0] < 3e-4 and errs[1] < 1e-6 and max(errs[2:]) < 1e-3
-    # different FP32 rounding orders; the continuation amplifies it in the r2c and NL outputs
-    cross = [rel(a, b) for a, b in zip(got[8], got[16])]
-    print("rows 8 vs 16", ["%.2e" % e for e in cross])
-    assert cross[0] < 3e-4 and cross[1] < 1e-6 and max(cross[2:]) < 1e-3
