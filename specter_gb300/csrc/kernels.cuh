@@ -54,6 +54,8 @@ struct GenericFFT {
         return fft_exec<T>(X, Y, B, d, sign);
     }
     static __device__ __forceinline__ int pos(int k, const Desc &) { return k; }
+    // pos(m + D) - pos(m) for every m, or -1 when that is not a constant
+    static __device__ __forceinline__ int pos_stride(int D, const Desc &) { return D; }
 };
 
 // OUTLINE = true calls the transforms out of line (kernels with many call sites).
@@ -96,6 +98,10 @@ struct FourStep {
         return X;
     }
     static __device__ __forceinline__ int pos(int k, const Desc &d) { return d.blue ? k : perm_pos<L1, L2>(k); }
+    // pos(m + D) - pos(m) for every m, or -1 when that is not a constant
+    static __device__ __forceinline__ int pos_stride(int D, const Desc &d) {
+        return d.blue ? D : (D % L1 == 0 ? D / L1 : -1);
+    }
 };
 
 // ---------------------------------------------------------------------------------
@@ -308,14 +314,16 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass(Geo g, typen
 
 // Build Z (H rows, natural order) for a C2R from the half spectrum S (nxh rows):
 // Z_k = (X_k + conj X_{H-k}) + i e^{+2 pi i k/nx} (X_k - conj X_{H-k}); Im X_0 = Im X_H = 0.
-// dx = 1 first multiplies the spectrum by i kx (the x derivative).
+// dx = 1 first multiplies the spectrum by i kx (the x derivative).  With e, o the two terms of
+// Z_k, Z_{H-k} = conj(e) + i conj(o): one thread forms the pair (k, H-k) from the same two
+// loads and one twiddle (k = 0 pairs X_0 with X_H and forms Z_0 only).
 template <typename T>
 __device__ __forceinline__ void c2r_pre(const Geo &g, const C2<T> *S, C2<T> *Z, int RB, int SP, int dx = 0) {
     const int lgRB = lg2(RB);
     using V = C2<T>;
     const V *xtw = (const V *)g.xtw;
-    const int H = g.H;
-    for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
+    const int H = g.H, Hh = H >> 1;
+    for (int idx = threadIdx.x; idx < (Hh + 1) * RB; idx += blockDim.x) {
         const int k = idx >> lgRB, r = idx & (RB - 1);
         V xk = S[k * SP + r], xm = S[(H - k) * SP + r];
         if (dx) {
@@ -329,11 +337,15 @@ __device__ __forceinline__ void c2r_pre(const Geo &g, const C2<T> *S, C2<T> *Z, 
         w.y = -w.y;  // exp(+2 pi i k / nx)
         const V o = cmul(csub(xk, xmc), w);
         Z[idx] = mk<T>(e.x - o.y, e.y + o.x);
+        if (k != 0 && 2 * k != H) Z[(H - k) * RB + r] = mk<T>(e.x + o.y, o.x - e.y);
     }
 }
 
 // From Z = FFT_H(packed real row), write the half spectrum X_0..X_H into S:
 //   X_k = (Z_k + conj Z_{H-k})/2 - (i/2) e^{-2 pi i k/nx} (Z_k - conj Z_{H-k}).
+// With e = Z_k + conj Z_{H-k} and t = e^{-2 pi i k/nx} (Z_k - conj Z_{H-k}), X_k = (e - i t)/2
+// and X_{H-k} = (conj(e) - i conj(t))/2: one thread forms the pair (k, H-k); k = 0 also gives
+// X_H.
 // Output k of Z sits at row E::pos(k), or at row k when NAT.
 template <typename T, class E, bool NAT = false>
 __device__ __forceinline__ void r2c_post(const Geo &g, const typename E::Desc &fd, const C2<T> *Z, C2<T> *S, int RB,
@@ -341,14 +353,16 @@ __device__ __forceinline__ void r2c_post(const Geo &g, const typename E::Desc &f
     const int lgRB = lg2(RB);
     using V = C2<T>;
     const V *xtw = (const V *)g.xtw;
-    const int H = g.H;
-    for (int idx = threadIdx.x; idx < (H + 1) * RB; idx += blockDim.x) {
+    const int H = g.H, Hh = H >> 1;
+    for (int idx = threadIdx.x; idx < (Hh + 1) * RB; idx += blockDim.x) {
         const int k = idx >> lgRB, r = idx & (RB - 1);
-        const int p0 = NAT ? k % H : E::pos(k % H, fd), p1 = NAT ? (H - k) % H : E::pos((H - k) % H, fd);
+        const int km = k ? H - k : 0;
+        const int p0 = NAT ? k : E::pos(k, fd), p1 = NAT ? km : E::pos(km, fd);
         const V zk = Z[p0 * RB + r], zm = cconj(Z[p1 * RB + r]);
         const V e = cadd(zk, zm), d = csub(zk, zm);
         const V t = cmul(d, __ldg(xtw + k));
         S[k * SP + r] = mk<T>((T)0.5 * (e.x + t.y), (T)0.5 * (e.y - t.x));
+        if (2 * k != H) S[(H - k) * SP + r] = mk<T>((T)0.5 * (e.x - t.y), (T)-0.5 * (e.y + t.x));
     }
 }
 
@@ -518,10 +532,14 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, 
             rows_load_async(S, xnl_input<T>(a, t + 1, tn, in_) + off, (unsigned)g.ldx, nxh, RB, nv, SP);
         }
         V *R = E::run(X, Y, RB, fd, +1);
+        // output m of R sits at row E::pos(m); m advances by D per iteration, so the row
+        // advances by a constant when the engine's permutation is affine along that stride
+        const int D = blockDim.x >> lgRB, ps = E::pos_stride(D, fd), r0 = threadIdx.x & (RB - 1);
         if (term < 2) {
-            for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
-                const int m = idx >> lgRB, r = idx & (RB - 1);
-                const V p = R[E::pos(m, fd) * RB + r];
+            int q = E::pos(threadIdx.x >> lgRB, fd) * RB + r0;
+            for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x, q += ps * RB) {
+                if (ps < 0) q = E::pos(idx >> lgRB, fd) * RB + r0;
+                const V p = R[q];
                 if (term < 0) {
                     U[i * H * RB + idx] = p;
                 } else if (term == 0) {
@@ -534,9 +552,9 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, 
             }
         } else {
             // (acc + u_z d/dz v_i) * tmp in place, forward transform from permuted order, R2C
-            for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
-                const int m = idx >> lgRB, r = idx & (RB - 1);
-                const int q = E::pos(m, fd) * RB + r;
+            int q = E::pos(threadIdx.x >> lgRB, fd) * RB + r0;
+            for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x, q += ps * RB) {
+                if (ps < 0) q = E::pos(idx >> lgRB, fd) * RB + r0;
                 const V u = U[2 * H * RB + idx], p = R[q], acc = A[idx];
                 R[q] = mk<T>((acc.x + u.x * p.x) * tmp, (acc.y + u.y * p.y) * tmp);
             }
