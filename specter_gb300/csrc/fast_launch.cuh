@@ -112,9 +112,12 @@ int xnl(Plan &P, const XNLArgs &a, double bytes) {
         if (t <= P.tile_cap[Plan::kTileX] && x_nl_elems<E>(P.tx4.d, P.nxh, P.H, t) * sizeof(float2) <= kMaxSmem) { rb = t; break; }
     if (!rb) return kNoFast;
     const size_t sm = x_nl_elems<E>(P.tx4.d, P.nxh, P.H, rb) * sizeof(float2);
-    smem_attr(k_x_nonlinear<float, E>, sm);
+    // the production x lengths (H = 256, 128) at 8 rows run a copy with the row count fixed
+    constexpr bool kFixed = L1 == 16 && (L2 == 16 || L2 == 8);
+    auto k = (kFixed && rb == 8) ? k_x_nonlinear<float, E, kFixed ? 8 : 0> : k_x_nonlinear<float, E>;
+    smem_attr(k, sm);
     Scope s(P, "x_nonlinear", bytes);
-    k_x_nonlinear<float, E><<<dim3(cdiv(a.nrows * P.ny, rb)), kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a.prepared(), rb);
+    k<<<dim3(cdiv(a.nrows * P.ny, rb)), kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a.prepared(), rb);
     return done("x_nonlinear");
 }
 }  // namespace

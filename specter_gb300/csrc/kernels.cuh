@@ -502,9 +502,12 @@ __host__ __device__ inline size_t x_nl_elems(const typename E::Desc &fd, int nxh
 // the permuted positions where the inverse transform left it, so the forward transform
 // starts from permuted input (E::run_perm) and no copy is needed.  Input t+1 is copied into
 // S while input t is transformed.
-template <typename T, class E>
-__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, typename E::Desc fd, XNLArgs a, int RB) {
-    const int lgRB = lg2(RB);
+// CRB: the rows per block when fixed at compile time (index arithmetic and the FFT's row offsets
+// become constants), else 0 and the runtime RBrt.
+template <typename T, class E, int CRB = 0>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, typename E::Desc fd, XNLArgs a, int RBrt) {
+    const int RB = CRB ? CRB : RBrt;
+    const int lgRB = CRB ? (CRB == 16 ? 4 : CRB == 8 ? 3 : CRB == 4 ? 2 : CRB == 2 ? 1 : 0) : lg2(RBrt);
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int H = g.H, L = fd.L, nxh = g.nxh, SP = RB + 1;
