@@ -77,9 +77,12 @@ int ypass(Plan &P, const YArgs &a0, int nf, int nplanes, double bytes) {
     const size_t per = ((size_t)P.ty4.d.L + (a.staged ? P.ny : 0)) * sizeof(float2);
     const int tk = P.capped(pick(per), Plan::kTileY);
     const size_t sm = per * tk;
-    smem_attr(k_y_pass<float, E>, sm);
+    // the production y lengths (512, 256) at tile width 16 run a copy with the width fixed
+    constexpr bool kFixed = L2 == 16 && (L1 == 32 || L1 == 16);
+    auto k = (kFixed && tk == 16) ? k_y_pass_t<float, E, kFixed ? 16 : 0> : k_y_pass_t<float, E, 0>;
+    smem_attr(k, sm);
     Scope s(P, a.sign < 0 ? "y_forward" : "y_inverse", bytes);
-    k_y_pass<float, E><<<dim3(cdiv(P.nxh, tk), nplanes, nf), kThreads, sm, P.stream>>>(P.geo, P.ty4.d, a.prepared(), tk);
+    k<<<dim3(cdiv(P.nxh, tk), nplanes, nf), kThreads, sm, P.stream>>>(P.geo, P.ty4.d, a.prepared(), tk);
     return done("y_pass");
 }
 

@@ -258,9 +258,11 @@ struct YArgs {
     YArgs prepared() const { YArgs b = *this; b.scale_f = (float)scale; return b; }
 };
 
-template <typename T, class E>
-__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass(Geo g, typename E::Desc fd, YArgs a, int TK) {
-    const int lgTK = lg2(TK);
+// CTK: the tile width when fixed at compile time, else 0 and the runtime TKrt
+template <typename T, class E, int CTK>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass_t(Geo g, typename E::Desc fd, YArgs a, int TKrt) {
+    const int TK = CTK ? CTK : TKrt;
+    const int lgTK = CTK ? (CTK == 16 ? 4 : CTK == 8 ? 3 : CTK == 4 ? 2 : CTK == 2 ? 1 : 0) : lg2(TKrt);
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     V *X = (V *)smem_raw, *Y = X + (size_t)fd.L * TK;

@@ -121,9 +121,9 @@ static int launch_y(Plan &P, const YArgs &a0, int nf, int nplanes) {
     for (int f = 0; f < nf; f++) bytes += cplx_rows(P, nplanes) * (1 + (a.out0[f] ? 1 : 0) + (a.out1[f] ? 1 : 0));
     const int fst = fast_y(P, a, nf, nplanes, bytes);
     if (fst != kNoFast) return fst;
-    set_smem(k_y_pass<T, GenericFFT<T>>, sm);
+    set_smem(k_y_pass_t<T, GenericFFT<T>, 0>, sm);
     Launch L(P, a.sign < 0 ? "y_forward" : "y_inverse", bytes);
-    k_y_pass<T, GenericFFT<T>><<<dim3(cdiv(P.nxh, tk), nplanes, nf), kThreads, sm, P.stream>>>(P.geo, P.ty.d, a.prepared(), tk);
+    k_y_pass_t<T, GenericFFT<T>, 0><<<dim3(cdiv(P.nxh, tk), nplanes, nf), kThreads, sm, P.stream>>>(P.geo, P.ty.d, a.prepared(), tk);
     return check_launch("y_pass");
 }
 
