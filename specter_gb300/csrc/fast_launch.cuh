@@ -52,9 +52,12 @@ int zinv(Plan &P, const ZInvArgs &a0, int nf, double bytes) {
     const size_t per = ((size_t)P.tz4.d.L + (a.staged ? P.nz : 0)) * sizeof(float2);
     const int tk = P.capped(pick(per), Plan::kTileZ);
     const size_t sm = per * tk;
-    smem_attr(k_z_inverse<float, E>, sm);
+    // the production z lengths (Bluestein 1080, 576) at tile width 8 run a copy with the width fixed
+    constexpr bool kFixed = (L1 == 36 && L2 == 30) || (L1 == 24 && L2 == 24);
+    auto k = (kFixed && tk == 8) ? k_z_inverse<float, E, kFixed ? 8 : 0> : k_z_inverse<float, E>;
+    smem_attr(k, sm);
     Scope s(P, "z_inverse", bytes);
-    k_z_inverse<float, E><<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz4.d, a.prepared(), tk);
+    k<<<dim3(cdiv(P.nxh, tk), P.ny, nf), kThreads, sm, P.stream>>>(P.geo, P.tz4.d, a.prepared(), tk);
     return done("z_inverse");
 }
 

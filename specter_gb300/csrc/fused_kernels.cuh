@@ -386,8 +386,9 @@ __global__ void __launch_bounds__(E::kWideThreads, 1) k_fused_velocity(Geo g, ty
 // Split form, part 1: one block per (column tile, component): the component's update and, for
 // vx and vy, the wall round trip; the result goes to W[c] (a stage buffer).  smem = Uc[nz][TK] +
 // FFT buffer(s): half the footprint of k_fused_velocity, so two blocks share an SM.
-template <typename T, class E>
-__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_vcomp(Geo g, typename E::Desc fd, FusedArgs a, int TK) {
+template <typename T, class E, int CTK = 0>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_vcomp(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
+    const int TK = CTK ? CTK : TKrt;  // CTK: the tile width fixed at compile time, else 0
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nz = g.nz, nzp = g.nzp;
@@ -414,8 +415,9 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_vcomp(Geo g, 
 }
 
 // Split form, part 2: the projection of the three components written by k_fused_vcomp.
-template <typename T, class E>
-__global__ void __launch_bounds__(kThreads, 2) k_fused_vproj(Geo g, typename E::Desc fd, FusedArgs a, int TK) {
+template <typename T, class E, int CTK = 0>
+__global__ void __launch_bounds__(kThreads, 2) k_fused_vproj(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
+    const int TK = CTK ? CTK : TKrt;  // CTK: the tile width fixed at compile time, else 0
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nz = g.nz;
@@ -435,8 +437,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_fused_vproj(Geo g, typename E::
 // ----------------------------------------------------------------------------------------------
 // scalar column kernel (Boussinesq): smem = Th[nz][TK] + E::kBuffers * L * TK
 // ----------------------------------------------------------------------------------------------
-template <typename T, class E>
-__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, typename E::Desc fd, FusedArgs a, int TK) {
+template <typename T, class E, int CTK = 0>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
+    const int TK = CTK ? CTK : TKrt;  // CTK: the tile width fixed at compile time, else 0
     const int lgTK = lg2(TK);
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -9,7 +9,8 @@ namespace sg {
 
 enum FusedKernel { kFusedVelocity = 0, kFusedTheta = 1, kFusedHerm = 2, kFusedVComp = 3, kFusedVProj = 4 };
 
-template <typename T, class E>
+// FIX: a tile width with its own compiled copy of the column kernels (0: none)
+template <typename T, class E, int FIX = 0>
 int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int which, double bytes) {
     const size_t es = sizeof(C2<T>);
     const size_t L = (size_t)fd.L;
@@ -45,15 +46,15 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
         if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k<<<dim3(cdiv(P.nxh, tk), P.ny), E::wide_threads(tk), sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
     } else if (which == kFusedVComp) {
-        auto k = k_fused_vcomp<T, E>;
+        auto k = (FIX && tk == FIX) ? k_fused_vcomp<T, E, FIX> : k_fused_vcomp<T, E>;
         if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k<<<dim3(cdiv(P.nxh, tk), P.ny, 3), kThreads, sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
     } else if (which == kFusedVProj) {
-        auto k = k_fused_vproj<T, E>;
+        auto k = (FIX && tk == FIX) ? k_fused_vproj<T, E, FIX> : k_fused_vproj<T, E>;
         if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k<<<dim3(cdiv(P.nxh, tk), P.ny), kThreads, sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
     } else if (which == kFusedTheta) {
-        auto k = k_fused_theta<T, E>;
+        auto k = (FIX && tk == FIX) ? k_fused_theta<T, E, FIX> : k_fused_theta<T, E>;
         if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k<<<dim3(cdiv(P.nxh, tk), P.ny), kThreads, sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
     } else {

@@ -121,8 +121,9 @@ struct ZInvArgs {
     ZInvArgs prepared() const { ZInvArgs b = *this; b.scale_f = (float)scale; return b; }
 };
 
-template <typename T, class E>
-__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_inverse(Geo g, typename E::Desc fd, ZInvArgs a, int TK) {
+template <typename T, class E, int CTK = 0>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_inverse(Geo g, typename E::Desc fd, ZInvArgs a, int TKrt) {
+    const int TK = CTK ? CTK : TKrt;  // CTK: the tile width fixed at compile time, else 0
     const int lgTK = lg2(TK);
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
