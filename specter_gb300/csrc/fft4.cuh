@@ -143,6 +143,56 @@ __device__ __forceinline__ void dft_reg_hz(C2<T> (&a)[N]) {
     RegStages<T, N, SIGN, 1, true>::run(a, b);
 }
 
+// ---- Good-Thomas (prime-factor) register DFTs -----------------------------------------------
+// For N = N1 * N2 with gcd(N1, N2) = 1 the DFT needs no twiddles: with the input map
+// n = (N2 n1 + N1 n2) mod N and the output map k = CRT(k1 mod N1, k2 mod N2), X[k] is the
+// N1 x N2 two-dimensional DFT of the reindexed input (Good 1958, Thomas 1963).  Both maps are
+// compile-time register renamings, so only the short DFTs remain: DFT30 = 2 x 3 x 5 and
+// DFT36 = 4 x 9 lose the 30 and 24 complex twiddle products of the mixed-radix chain.  Lengths
+// without a coprime split (powers of two, 9, 27) use the Stockham chain (dft_reg).
+constexpr int gcd_c(int a, int b) { return b ? gcd_c(b, a % b) : a; }
+constexpr int inv_mod_c(int a, int m) {
+    int x = 1;
+    while (x < m && (a * x) % m != 1) x++;
+    return x;
+}
+// first factor of a coprime split of N (the largest prime-power factor first), or 0
+constexpr int pfa_n1(int N) {
+    const int c[] = {16, 8, 4, 9, 27, 5, 3, 2};
+    for (int i = 0; i < 8; i++)
+        if (c[i] < N && N % c[i] == 0 && gcd_c(c[i], N / c[i]) == 1) return c[i];
+    return 0;
+}
+
+template <typename T, int N, int SIGN>
+__device__ __forceinline__ void dft_pfa(C2<T> (&a)[N]) {
+    constexpr int N1 = pfa_n1(N);
+    if constexpr (N1 == 0) {
+        if constexpr (N == 2 || N == 3 || N == 4 || N == 5) butterfly<T, N>(a, SIGN, nullptr, 0);
+        else dft_reg<T, N, SIGN>(a);
+    } else {
+        constexpr int N2 = N / N1;
+        constexpr int e1 = N2 * inv_mod_c(N2 % N1, N1);  // k = (e1 k1 + e2 k2) mod N
+        constexpr int e2 = N1 * inv_mod_c(N1 % N2, N2);
+        C2<T> y[N1][N2];
+#pragma unroll
+        for (int n1 = 0; n1 < N1; n1++)
+#pragma unroll
+            for (int n2 = 0; n2 < N2; n2++) y[n1][n2] = a[(N2 * n1 + N1 * n2) % N];
+#pragma unroll
+        for (int n1 = 0; n1 < N1; n1++) dft_pfa<T, N2, SIGN>(y[n1]);
+#pragma unroll
+        for (int k2 = 0; k2 < N2; k2++) {
+            C2<T> col[N1];
+#pragma unroll
+            for (int n1 = 0; n1 < N1; n1++) col[n1] = y[n1][k2];
+            dft_pfa<T, N1, SIGN>(col);
+#pragma unroll
+            for (int k1 = 0; k1 < N1; k1++) a[(e1 * k1 + e2 * k2) % N] = col[k1];
+        }
+    }
+}
+
 // twiddle w_L^{SIGN * t} from a global table tw[t] = exp(-2 pi i t / L)
 template <typename T, int SIGN>
 __device__ __forceinline__ C2<T> gtw(const C2<T> *tw, int t) {
@@ -162,7 +212,7 @@ __device__ __forceinline__ C2<T> gtw(const C2<T> *tw, int t) {
 constexpr int ct_lg2(int b) { return b <= 1 ? 0 : 1 + ct_lg2(b / 2); }
 
 // ---- natural -> permuted (steps A, B) ---------------------------------------------------------
-template <typename T, int L1, int L2, int SIGN, int CB>
+template <typename T, int L1, int L2, int SIGN, int CB, bool PFA = true>
 __device__ __forceinline__ void fft4_np_impl(C2<T> *X, int Brt, const FFT4Desc &d) {
     const int B = CB ? CB : Brt;
     const int lgB = CB ? ct_lg2(CB) : lg2(Brt);
@@ -173,7 +223,7 @@ __device__ __forceinline__ void fft4_np_impl(C2<T> *X, int Brt, const FFT4Desc &
         C2<T> a[L1];
 #pragma unroll
         for (int n1 = 0; n1 < L1; n1++) a[n1] = X[(n2 + L2 * n1) * B + c];
-        dft_reg<T, L1, SIGN>(a);
+        if constexpr (PFA) dft_pfa<T, L1, SIGN>(a); else dft_reg<T, L1, SIGN>(a);
 #pragma unroll
         for (int k1 = 1; k1 < L1; k1++) a[k1] = cmul(a[k1], gtw<T, SIGN>(tw4, n2 * L1 + k1));
 #pragma unroll
@@ -185,7 +235,7 @@ __device__ __forceinline__ void fft4_np_impl(C2<T> *X, int Brt, const FFT4Desc &
         C2<T> b[L2];
 #pragma unroll
         for (int n2 = 0; n2 < L2; n2++) b[n2] = X[(L2 * k1 + n2) * B + c];
-        dft_reg<T, L2, SIGN>(b);
+        if constexpr (PFA) dft_pfa<T, L2, SIGN>(b); else dft_reg<T, L2, SIGN>(b);
 #pragma unroll
         for (int k2 = 0; k2 < L2; k2++) X[(L2 * k1 + k2) * B + c] = b[k2];
     }
@@ -200,7 +250,7 @@ __device__ __forceinline__ void fft4_np(C2<T> *X, int B, const FFT4Desc &d) {
 }
 
 // ---- permuted -> natural (steps B', A') -------------------------------------------------------
-template <typename T, int L1, int L2, int SIGN, int CB>
+template <typename T, int L1, int L2, int SIGN, int CB, bool PFA = true>
 __device__ __forceinline__ void fft4_pn_impl(C2<T> *X, int Brt, const FFT4Desc &d) {
     const int B = CB ? CB : Brt;
     const int lgB = CB ? ct_lg2(CB) : lg2(Brt);
@@ -210,7 +260,7 @@ __device__ __forceinline__ void fft4_pn_impl(C2<T> *X, int Brt, const FFT4Desc &
         C2<T> b[L2];
 #pragma unroll
         for (int k2 = 0; k2 < L2; k2++) b[k2] = X[(L2 * k1 + k2) * B + c];
-        dft_reg<T, L2, SIGN>(b);
+        if constexpr (PFA) dft_pfa<T, L2, SIGN>(b); else dft_reg<T, L2, SIGN>(b);
 #pragma unroll
         for (int m2 = 1; m2 < L2; m2++) b[m2] = cmul(b[m2], gtw<T, SIGN>(tw4, m2 * L1 + k1));
 #pragma unroll
@@ -222,7 +272,7 @@ __device__ __forceinline__ void fft4_pn_impl(C2<T> *X, int Brt, const FFT4Desc &
         C2<T> a[L1];
 #pragma unroll
         for (int k1 = 0; k1 < L1; k1++) a[k1] = X[(L2 * k1 + m2) * B + c];
-        dft_reg<T, L1, SIGN>(a);
+        if constexpr (PFA) dft_pfa<T, L1, SIGN>(a); else dft_reg<T, L1, SIGN>(a);
 #pragma unroll
         for (int m1 = 0; m1 < L1; m1++) X[(m2 + L2 * m1) * B + c] = a[m1];
     }
@@ -248,7 +298,11 @@ __device__ __forceinline__ int perm_pos(int k) { return L2 * (k % L1) + k / L1; 
 // are built): in step A the inputs n1 >= L1/2 are the zero padding and in step A' the outputs
 // m1 >= L1/2 are discarded, so both steps work on half of their DFT_L1 ends.
 // CB: the tile width when known at compile time, else 0
-template <typename T, int L1, int L2, int CB>
+// PFA: the inner DFTs of steps B and A' use the prime-factor form (dft_pfa); the out-of-line
+// copies called by the fused column kernels (fft4_bluestein_ni, fft4_np_ni) keep the
+// mixed-radix form, whose smaller register footprint costs the callers fewer saves around the
+// call (measured: fused_theta 10 % slower with the prime-factor form, z_inverse 5 % faster).
+template <typename T, int L1, int L2, int CB, bool PFA>
 __device__ __forceinline__ void fft4_bluestein_impl(C2<T> *X, int Brt, const FFT4Desc &d, int sign) {
     static_assert(L1 % 2 == 0, "Bluestein four-step needs an even L1");
     constexpr int kH = L1 / 2;
@@ -286,10 +340,10 @@ __device__ __forceinline__ void fft4_bluestein_impl(C2<T> *X, int Brt, const FFT
         C2<T> b[L2];
 #pragma unroll
         for (int n2 = 0; n2 < L2; n2++) b[n2] = X[(L2 * k1 + n2) * B + c];
-        dft_reg<T, L2, -1>(b);
+        if constexpr (PFA) dft_pfa<T, L2, -1>(b); else dft_reg<T, L2, -1>(b);
 #pragma unroll
         for (int k2 = 0; k2 < L2; k2++) b[k2] = cmul(b[k2], __ldg(filt + k1 * L2 + k2));
-        dft_reg<T, L2, +1>(b);
+        if constexpr (PFA) dft_pfa<T, L2, +1>(b); else dft_reg<T, L2, +1>(b);
 #pragma unroll
         for (int m2 = 1; m2 < L2; m2++) b[m2] = cmul(b[m2], gtw<T, +1>(tw4, m2 * L1 + k1));
 #pragma unroll
@@ -302,7 +356,7 @@ __device__ __forceinline__ void fft4_bluestein_impl(C2<T> *X, int Brt, const FFT
         C2<T> a[L1];
 #pragma unroll
         for (int k1 = 0; k1 < L1; k1++) a[k1] = X[(L2 * k1 + m2) * B + c];
-        dft_reg<T, L1, +1>(a);
+        if constexpr (PFA) dft_pfa<T, L1, +1>(a); else dft_reg<T, L1, +1>(a);
 #pragma unroll
         for (int m1 = 0; m1 < kH; m1++) {
             const int pos = m2 + L2 * m1;
@@ -316,11 +370,11 @@ __device__ __forceinline__ void fft4_bluestein_impl(C2<T> *X, int Brt, const FFT
     __syncthreads();
 }
 
-template <typename T, int L1, int L2>
+template <typename T, int L1, int L2, bool PFA = true>
 __device__ __forceinline__ void fft4_bluestein_body(C2<T> *X, int B, const FFT4Desc &d, int sign) {
-    if (B == 8) fft4_bluestein_impl<T, L1, L2, 8>(X, 8, d, sign);
-    else if (B == 16) fft4_bluestein_impl<T, L1, L2, 16>(X, 16, d, sign);
-    else fft4_bluestein_impl<T, L1, L2, 0>(X, B, d, sign);
+    if (B == 8) fft4_bluestein_impl<T, L1, L2, 8, PFA>(X, 8, d, sign);
+    else if (B == 16) fft4_bluestein_impl<T, L1, L2, 16, PFA>(X, 16, d, sign);
+    else fft4_bluestein_impl<T, L1, L2, 0, PFA>(X, B, d, sign);
 }
 
 template <typename T, int L1, int L2, int SIGN>
@@ -332,11 +386,11 @@ __device__ __forceinline__ void fft4_bluestein(C2<T> *X, int B, const FFT4Desc &
 // one body in the instruction stream instead of one per call site.
 template <typename T, int L1, int L2>
 __device__ __noinline__ void fft4_bluestein_ni(C2<T> *X, int B, const FFT4Desc &d, int sign) {
-    fft4_bluestein_body<T, L1, L2>(X, B, d, sign);
+    fft4_bluestein_body<T, L1, L2, false>(X, B, d, sign);
 }
 template <typename T, int L1, int L2, int SIGN>
 __device__ __noinline__ void fft4_np_ni(C2<T> *X, int B, const FFT4Desc &d) {
-    fft4_np<T, L1, L2, SIGN>(X, B, d);
+    fft4_np_impl<T, L1, L2, SIGN, 0, false>(X, B, d);
 }
 
 }  // namespace sg
