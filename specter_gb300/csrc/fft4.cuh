@@ -298,10 +298,11 @@ __device__ __forceinline__ int perm_pos(int k) { return L2 * (k % L1) + k / L1; 
 // are built): in step A the inputs n1 >= L1/2 are the zero padding and in step A' the outputs
 // m1 >= L1/2 are discarded, so both steps work on half of their DFT_L1 ends.
 // CB: the tile width when known at compile time, else 0
-// PFA: the inner DFTs of steps B and A' use the prime-factor form (dft_pfa); the out-of-line
+// Step B's DFTs always use the prime-factor form (dft_pfa).  PFA: step A' too; the out-of-line
 // copies called by the fused column kernels (fft4_bluestein_ni, fft4_np_ni) keep the
-// mixed-radix form, whose smaller register footprint costs the callers fewer saves around the
-// call (measured: fused_theta 10 % slower with the prime-factor form, z_inverse 5 % faster).
+// mixed-radix DFT there, whose smaller register footprint costs the callers fewer saves around
+// the call (measured with the prime-factor form in every step: fused_theta 10 % slower,
+// z_inverse 5 % faster; in step B only: fused_vcomp and fused_theta 2-3 % faster).
 template <typename T, int L1, int L2, int CB, bool PFA>
 __device__ __forceinline__ void fft4_bluestein_impl(C2<T> *X, int Brt, const FFT4Desc &d, int sign) {
     static_assert(L1 % 2 == 0, "Bluestein four-step needs an even L1");
@@ -340,10 +341,10 @@ __device__ __forceinline__ void fft4_bluestein_impl(C2<T> *X, int Brt, const FFT
         C2<T> b[L2];
 #pragma unroll
         for (int n2 = 0; n2 < L2; n2++) b[n2] = X[(L2 * k1 + n2) * B + c];
-        if constexpr (PFA) dft_pfa<T, L2, -1>(b); else dft_reg<T, L2, -1>(b);
+        dft_pfa<T, L2, -1>(b);
 #pragma unroll
         for (int k2 = 0; k2 < L2; k2++) b[k2] = cmul(b[k2], __ldg(filt + k1 * L2 + k2));
-        if constexpr (PFA) dft_pfa<T, L2, +1>(b); else dft_reg<T, L2, +1>(b);
+        dft_pfa<T, L2, +1>(b);
 #pragma unroll
         for (int m2 = 1; m2 < L2; m2++) b[m2] = cmul(b[m2], gtw<T, +1>(tw4, m2 * L1 + k1));
 #pragma unroll
