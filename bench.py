@@ -370,7 +370,8 @@ def main():
                 "clocks": clocks.summary(),
                 "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                         "steps": Ke, "median_ms_per_step": round(1e3 * statistics.median(tsteps), 3),
-                        "mean_ms_per_step": round(1e3 * statistics.mean(tsteps), 3)},
+                        "mean_ms_per_step": round(1e3 * statistics.mean(tsteps), 3),
+                        "ms_per_step_each": [round(1e3 * t, 1) for t in tsteps]},
                 "gpu_launches": launches}
         if not args.no_cpu and not args.fp64 and world == 1:
             v, cores, sample = cpu_baseline(1, 0)
