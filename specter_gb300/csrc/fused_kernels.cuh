@@ -251,8 +251,12 @@ __device__ void vel_project(const Geo &g, const typename E::Desc &fd, const Fuse
                 const double vr = (double)Cc.x, vi = (double)Cc.y;
                 const double2 w = wtw[k];
                 s0.x += vr; s0.y += vi;
-                s1.x += vr * w.x - vi * w.y;
-                s1.y += vr * w.y + vi * w.x;
+                // the top wall: s1 += v w as four FP64 fused multiply-adds (the FP64 pipe, two
+                // operations per clock per SM, bounds this loop)
+                s1.x = fma(vr, w.x, s1.x);
+                s1.x = fma(-vi, w.y, s1.x);
+                s1.y = fma(vr, w.y, s1.y);
+                s1.y = fma(vi, w.x, s1.y);
             }
         }
         // sum over the threads of a column: shuffles within each warp (the lanes of column c are

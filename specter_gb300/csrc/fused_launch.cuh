@@ -50,7 +50,9 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
         if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k<<<dim3(cdiv(P.nxh, tk), P.ny, 3), kThreads, sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
     } else if (which == kFusedVProj) {
-        auto k = (FIX && tk == FIX) ? k_fused_vproj<T, E, FIX> : k_fused_vproj<T, E>;
+        // the projection holds three components, so at the same cap it runs half the width of
+        // the other column kernels: its own fixed-width copy at FIX / 2
+        auto k = (FIX && tk == FIX) ? k_fused_vproj<T, E, FIX> : (FIX && tk == FIX / 2) ? k_fused_vproj<T, E, FIX / 2> : k_fused_vproj<T, E>;
         if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         k<<<dim3(cdiv(P.nxh, tk), P.ny), kThreads, sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
     } else if (which == kFusedTheta) {
