@@ -241,7 +241,13 @@ __device__ void vel_project(const Geo &g, const typename E::Desc &fd, const Fuse
                 const T k2 = kx_ * kx_ + ky_ * ky_ + kz_ * kz_;
                 V A = U[idx], B = U[tile + idx], Cc = U[2 * tile + idx];
                 const V s = mk<T>(kx_ * A.x + ky_ * B.x + kz_ * Cc.x, kx_ * A.y + ky_ * B.y + kz_ * Cc.y);
-                V D = mk<T>(s.y / k2, -s.x / k2);
+                V D;
+                if constexpr (sizeof(T) == 4) {  // FP32-bulk: one division per point
+                    const T ik2 = (T)1 / k2;
+                    D = mk<T>(s.y * ik2, -s.x * ik2);
+                } else {
+                    D = mk<T>(s.y / k2, -s.x / k2);
+                }
                 if (k == 0 && ky == 0 && kx0 + c == 0) D = mk<T>(0, 0);
                 A = csub(A, cimk(kx_, D));
                 B = csub(B, cimk(ky_, D));
