@@ -212,10 +212,10 @@ __device__ __forceinline__ C2<T> gtw(const C2<T> *tw, int t) {
 constexpr int ct_lg2(int b) { return b <= 1 ? 0 : 1 + ct_lg2(b / 2); }
 
 // ---- natural -> permuted (steps A, B) ---------------------------------------------------------
-template <typename T, int L1, int L2, int SIGN, int CB, bool PFA = true>
-__device__ __forceinline__ void fft4_np_impl(C2<T> *X, int Brt, const FFT4Desc &d) {
-    const int B = CB ? CB : Brt;
-    const int lgB = CB ? ct_lg2(CB) : lg2(Brt);
+// PFA: prime-factor register DFTs (dft_pfa) instead of the mixed-radix chain (dft_reg)
+template <typename T, int L1, int L2, int SIGN, bool PFA = true>
+__device__ __forceinline__ void fft4_np_impl(C2<T> *X, int B, const FFT4Desc &d) {
+    const int lgB = lg2(B);
     constexpr int L = L1 * L2;
     const C2<T> *tw4 = (const C2<T> *)d.tw4;
     for (int idx = threadIdx.x; idx < B * L2; idx += blockDim.x) {
@@ -243,17 +243,18 @@ __device__ __forceinline__ void fft4_np_impl(C2<T> *X, int Brt, const FFT4Desc &
     (void)L;
 }
 
-// (the x and y passes measured slower with the width-specialised copies: runtime width only)
+// Three width-specialised bodies per call site made the x and y passes slower; instead the
+// kernels come in fixed-width copies whose constant width reaches these bodies by inlining.
 template <typename T, int L1, int L2, int SIGN>
 __device__ __forceinline__ void fft4_np(C2<T> *X, int B, const FFT4Desc &d) {
-    fft4_np_impl<T, L1, L2, SIGN, 0>(X, B, d);
+    fft4_np_impl<T, L1, L2, SIGN>(X, B, d);
 }
 
 // ---- permuted -> natural (steps B', A') -------------------------------------------------------
-template <typename T, int L1, int L2, int SIGN, int CB, bool PFA = true>
-__device__ __forceinline__ void fft4_pn_impl(C2<T> *X, int Brt, const FFT4Desc &d) {
-    const int B = CB ? CB : Brt;
-    const int lgB = CB ? ct_lg2(CB) : lg2(Brt);
+// PFA: prime-factor register DFTs (dft_pfa) instead of the mixed-radix chain (dft_reg)
+template <typename T, int L1, int L2, int SIGN, bool PFA = true>
+__device__ __forceinline__ void fft4_pn_impl(C2<T> *X, int B, const FFT4Desc &d) {
+    const int lgB = lg2(B);
     const C2<T> *tw4 = (const C2<T> *)d.tw4;
     for (int idx = threadIdx.x; idx < B * L1; idx += blockDim.x) {
         const int c = idx & (B - 1), k1 = idx >> lgB;
@@ -281,7 +282,7 @@ __device__ __forceinline__ void fft4_pn_impl(C2<T> *X, int Brt, const FFT4Desc &
 
 template <typename T, int L1, int L2, int SIGN>
 __device__ __forceinline__ void fft4_pn(C2<T> *X, int B, const FFT4Desc &d) {
-    fft4_pn_impl<T, L1, L2, SIGN, 0>(X, B, d);
+    fft4_pn_impl<T, L1, L2, SIGN>(X, B, d);
 }
 
 // position in the permuted layout of frequency k
@@ -391,7 +392,7 @@ __device__ __noinline__ void fft4_bluestein_ni(C2<T> *X, int B, const FFT4Desc &
 }
 template <typename T, int L1, int L2, int SIGN>
 __device__ __noinline__ void fft4_np_ni(C2<T> *X, int B, const FFT4Desc &d) {
-    fft4_np_impl<T, L1, L2, SIGN, 0, false>(X, B, d);
+    fft4_np_impl<T, L1, L2, SIGN, false>(X, B, d);
 }
 
 }  // namespace sg
