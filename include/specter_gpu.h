@@ -90,7 +90,9 @@ int specter_fields_download(int n, specter_field *const *fields, void *const *ho
 int specter_field_copy(specter_field *dst, const specter_field *src);
 int specter_field_zero(specter_field *f);
 /* upload/download of a contiguous batch of host rows is the same call with a pinned buffer;
- * the device pointer of a field, for interop (layout: see the design doc, kx fastest) */
+ * the device pointer of a field, for interop.  Device layout: complex fields are
+ * f[(z * ny + ky) * ldx + kx] (kx fastest, row stride ldx = nx/2+1 rounded up to 8, info[6] of
+ * specter_plan_info); real fields are r[(z * ny + y) * nx + x]. */
 int specter_field_device_ptr(specter_field *f, void **ptr, long long *bytes);
 
 /* ---- fftp (src/fftp/fftp.fpp) */
