@@ -118,9 +118,11 @@ __device__ __forceinline__ ColTile col_tile(const Geo &g, int TK) {
 // for the calling thread) and, when buoy, a copy of theta's tile is in flight into Uc.  Forward
 // z transform with continuation, + 2 Om x v (ROTBOUSS), - xmom theta (buoy), fc_filter, then
 // Uc = cold + dt (nu lap(vin) - n) / o  (hd_rkstep2.f90:1-32, bouss_rkstep2.f90:1-48).
+// to_x: leave the updated component in the FFT buffer X (natural rows) instead of Uc, for a
+// caller that transforms it next (vel_walls with in_x)
 template <typename T, class E>
 __device__ void vel_update(const Geo &g, const typename E::Desc &fd, const FusedArgs &a, const ColTile &t, int c3,
-                           C2<T> *Uc, C2<T> *X, C2<T> *Y, bool buoy) {
+                           C2<T> *Uc, C2<T> *X, C2<T> *Y, bool buoy, bool to_x = false) {
     using V = C2<T>;
     const int nz = g.nz, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
     const int tile = nz * TK;
@@ -165,15 +167,16 @@ __device__ void vel_update(const Geo &g, const typename E::Desc &fd, const Fused
     if (stage2) tile_load_async(X + tile, cold + t.col0, t.zs, nz, TK, nv);
     async_wait();
     __syncthreads();
+    V *dst = to_x ? X : Uc;  // X[idx]: each thread reads its own element first
     for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
         const int k = idx >> lgTK, c = idx & (TK - 1);
-        if (c >= nv) { Uc[idx] = mk<T>(0, 0); continue; }
+        if (c >= nv) { dst[idx] = mk<T>(0, 0); continue; }
         const int kx = kx0 + c;
         const T k2 = g.KX<T>(kx) * g.KX<T>(kx) + g.KY<T>(ky) * g.KY<T>(ky) + g.KZ<T>(k) * g.KZ<T>(k);
         const V v = X[idx], cv = stage2 ? X[tile + idx] : cold[fidx<T>(g, k, ky, kx)];
         const V n = Uc[idx];
         const V lap = cscale(v, -k2);
-        Uc[idx] = mk<T>(cv.x + dt * (nu * lap.x - n.x) * rmp, cv.y + dt * (nu * lap.y - n.y) * rmp);
+        dst[idx] = mk<T>(cv.x + dt * (nu * lap.x - n.x) * rmp, cv.y + dt * (nu * lap.y - n.y) * rmp);
     }
     __syncthreads();
 }
@@ -181,16 +184,23 @@ __device__ void vel_update(const Geo &g, const typename E::Desc &fd, const Fused
 // goto_domain_w_boundaries, noslip_z, goto_3d_fourier for component c3 in {0, 1}
 // (boundary_mod.fpp:72-194, vboundary.f90:154-211): z-inverse, 1/nz on the physical rows, wall
 // rows from the previous stage's pressure, continuation and z-forward; Uc in and out.
+// in_x: the component is already in X (vel_update with to_x); wout: store the result to this
+// global field instead of Uc.  With a single in-place FFT buffer in natural order (the
+// Bluestein four-step engine) the physical rows are finished in X itself.
 template <typename T, class E>
 __device__ void vel_walls(const Geo &g, const typename E::Desc &fd, const FusedArgs &a, const ColTile &t, int c3,
-                          C2<T> *Uc, C2<T> *X, C2<T> *Y) {
+                          C2<T> *Uc, C2<T> *X, C2<T> *Y, bool in_x = false, C2<T> *wout = nullptr) {
     using V = C2<T>;
     const int nz = g.nz, nzp = g.nzp, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
     const V *pr = (const V *)a.pr;
     const T wall_tmp = pick<T>(a.wall_tmp, a.f_wall_tmp), inz = (T)1 / (T)nz;
-    for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) X[idx] = Uc[idx];
-    __syncthreads();
+    if (!in_x) {
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) X[idx] = Uc[idx];
+        __syncthreads();
+    }
     V *R = E::run(X, Y, TK, fd, +1);
+    const bool inplace = R == X && fd.blue;  // natural order in X
+    V *P = inplace ? X : Uc;                 // physical rows, natural order
     for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
         const int k = idx >> lgTK, c = idx & (TK - 1);
         V v = cscale(R[E::pos(k, fd) * TK + c], inz);
@@ -200,14 +210,23 @@ __device__ void vel_walls(const Geo &g, const typename E::Desc &fd, const FusedA
             v = cscale(cimk(c3 == 0 ? g.KX<T>(kx) : g.KY<T>(ky), p), wall_tmp);
             if (kx == 0 && ky == 0) v = mk<T>((T)((double)g.nx * g.ny * a.vb[(k == 0 ? 0 : 2) + c3]), (T)0);
         }
-        Uc[idx] = v;  // physical rows, natural order (temporary)
+        P[idx] = v;
     }
     __syncthreads();
-    for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Uc[idx];
-    __syncthreads();
+    if (!inplace) {
+        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Uc[idx];
+        __syncthreads();
+    }
     fc_continuation<T>(g, X, TK);
     __syncthreads();
     R = E::run(X, Y, TK, fd, -1);
+    if (wout) {
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+            const int k = idx >> lgTK, c = idx & (TK - 1);
+            if (c < nv) wout[fidx<T>(g, k, ky, kx0 + c)] = R[E::pos(k, fd) * TK + c];
+        }
+        return;
+    }
     for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
         const int k = idx >> lgTK, c = idx & (TK - 1);
         Uc[idx] = R[E::pos(k, fd) * TK + c];
@@ -415,9 +434,14 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_vcomp(Geo g, 
     } else {
         async_wait();
     }
-    vel_update<T, E>(g, fd, a, t, c3, Uc, X, Y, buoy);
-    if (c3 < 2) vel_walls<T, E>(g, fd, a, t, c3, Uc, X, Y);
     V *w = (V *)a.work[c3];
+    if (c3 < 2) {
+        // the update stays in the FFT buffer and the wall round trip stores its result directly
+        vel_update<T, E>(g, fd, a, t, c3, Uc, X, Y, buoy, true);
+        vel_walls<T, E>(g, fd, a, t, c3, Uc, X, Y, true, w);
+        return;
+    }
+    vel_update<T, E>(g, fd, a, t, c3, Uc, X, Y, buoy);
     for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
         const int k = idx >> t.lgTK, c = idx & (TK - 1);
         if (c < t.nv) w[fidx<T>(g, k, t.ky, t.kx0 + c)] = Uc[idx];
