@@ -521,30 +521,35 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
         if (stage2) tile_load_async(X + tile, cold + col0, zs, nz, TK, nv);
         async_wait();
         __syncthreads();
+        // the updated theta goes straight into the FFT buffer (each thread reads its element first)
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
             const int k = idx >> lgTK, c = idx & (TK - 1);
-            if (c >= nv) { Th[idx] = mk<T>(0, 0); continue; }
+            if (c >= nv) { X[idx] = mk<T>(0, 0); continue; }
             const int kx = kx0 + c;
             const T k2 = g.KX<T>(kx) * g.KX<T>(kx) + g.KY<T>(ky) * g.KY<T>(ky) + g.KZ<T>(k) * g.KZ<T>(k);
             const V t = X[idx], cv = stage2 ? X[tile + idx] : cold[colq(k, c)];
             const V n = Th[idx];
             const V lap = cscale(t, -k2);
-            Th[idx] = mk<T>(cv.x + dt * (kap * lap.x - n.x) * rmp, cv.y + dt * (kap * lap.y - n.y) * rmp);
+            X[idx] = mk<T>(cv.x + dt * (kap * lap.x - n.x) * rmp, cv.y + dt * (kap * lap.y - n.y) * rmp);
         }
         __syncthreads();
     }
-    // 2. s_imposebc (IFFT, 1/nz, walls = 0, continuation + FFT), then fc_filter
+    // 2. s_imposebc (IFFT, 1/nz, walls = 0, continuation + FFT), then fc_filter.  With one
+    //    in-place buffer in natural order (the Bluestein four-step engine) every step finishes
+    //    in X; otherwise through Th.
     {
-        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) X[idx] = Th[idx];
-        __syncthreads();
         V *R = E::run(X, Y, TK, fd, +1);
+        bool inplace = R == X && fd.blue;
+        V *P = inplace ? X : Th;
         for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
             const int k = idx >> lgTK, c = idx & (TK - 1);
-            Th[idx] = (k == 0 || k == nzp - 1) ? mk<T>(0, 0) : cscale(R[E::pos(k, fd) * TK + c], inz);
+            P[idx] = (k == 0 || k == nzp - 1) ? mk<T>(0, 0) : cscale(R[E::pos(k, fd) * TK + c], inz);
         }
         __syncthreads();
-        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Th[idx];
-        __syncthreads();
+        if (!inplace) {
+            for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Th[idx];
+            __syncthreads();
+        }
         fc_continuation<T>(g, X, TK);
         __syncthreads();
         R = E::run(X, Y, TK, fd, -1);
@@ -556,6 +561,8 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
             }
             return;
         }
+        inplace = R == X && fd.blue;
+        P = inplace ? X : Th;
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
             const int k = idx >> lgTK, c = idx & (TK - 1);
             const int kx = min(kx0 + c, g.nxh - 1);
@@ -563,27 +570,33 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
             v = cscale(v, g.FX<T>(kx));
             v = cscale(v, g.FY<T>(ky));
             v = cscale(v, g.FZ<T>(k));
-            Th[idx] = v;
+            P[idx] = v;
         }
         __syncthreads();
+        if (!inplace) {
+            for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) X[idx] = Th[idx];
+            __syncthreads();
+        }
     }
     // 3. c2r -> /(nx ny nz) -> r2c: z-inverse and 1/nz here; kx = 0 and nx/2 go to the side buffer
     {
-        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) X[idx] = Th[idx];
-        __syncthreads();
         V *R = E::run(X, Y, TK, fd, +1);
+        const bool inplace = R == X && fd.blue;
+        V *P = inplace ? X : Th;
         V *side = (V *)a.side;
         for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
             const int k = idx >> lgTK, c = idx & (TK - 1);
             const V v = cscale(R[E::pos(k, fd) * TK + c], inz);
-            Th[idx] = v;
+            P[idx] = v;
             const int kx = kx0 + c;
             if (c < nv && (kx == 0 || kx == g.nxh - 1))
                 side[((unsigned)(kx == 0 ? 0 : 1) * g.ny + ky) * nzp + k] = v;
         }
         __syncthreads();
-        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Th[idx];
-        __syncthreads();
+        if (!inplace) {
+            for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Th[idx];
+            __syncthreads();
+        }
         fc_continuation<T>(g, X, TK);
         __syncthreads();
         R = E::run(X, Y, TK, fd, -1);
