@@ -131,3 +131,46 @@ def test_stage_fp32(pair32, solver):
     cons = [rel(a, b) for a, b in zip(outs[True], outs[False])]
     print("fused vs reference sequence", ["%.2e" % e for e in cons])
     assert max(cons) < 1e-3
+
+
+@pytest.mark.parametrize("shape", [(256, 32, 33), (512, 16, 33)], ids=["H128", "H256"])
+def test_x_pass_eight_rows(shape):
+    """At 8 rows (the autotuned width of the headline grid) the nonlinear x pass of H = 128 and 256
+    runs the copy compiled with the row count fixed; at 16 rows the runtime-width copy.  Both
+    against the oracle and each other, and a full fused RK2 stage at 8 rows against the oracle."""
+    from specter_gb300 import api
+    nx, ny, nzp = shape
+    plan, g = make_pair(nx, ny, nzp, 2.0, precision=1)
+    rng = np.random.default_rng(16)
+    v = [smooth_spectral(g, rng) for _ in range(3)]
+    th = smooth_spectral(g, rng)
+    ref_nl = g.gradre(*v)
+    ref_th = g.advect(*v, th)
+    got = {}
+    for cap in (8, 16):
+        api.set_tile_caps(plan, [16, 16, cap, 16])
+        nl = [plan.field() for _ in range(3)]
+        fv = [plan.field(data=x) for x in v]
+        api.gradre(plan, *fv, *nl)
+        fe = plan.field()
+        api.advect(plan, *fv, plan.field(data=th), fe)
+        got[cap] = [f.download() for f in nl] + [fe.download()]
+        errs = [rel(a, b) for a, b in zip(got[cap], list(ref_nl) + [ref_th])]
+        print(cap, ["%.2e" % e for e in errs])
+        assert max(errs) < 1e-3
+    cross = [rel(a, b) for a, b in zip(got[8], got[16])]
+    print("rows 8 vs 16", ["%.2e" % e for e in cross])
+    assert max(cross) < 1e-3
+    # one fused BOUSS RK2 step with the 8-row x pass
+    api.set_tile_caps(plan, [16, 16, 8, 16])
+    kw = dict(dt=1e-4, nu=1e-3, ord=2, kappa=1e-3)
+    pr = np.zeros(g.sshape, complex)
+    ref = g.run(g.params(**kw), 1, *v, pr, th=th)
+    s = api.Solver(plan, 1, fused=True, **kw)
+    for fld, x in zip((s.vx, s.vy, s.vz), v):
+        fld.upload(x)
+    s.th.upload(th)
+    s.step(1)
+    errs = [rel(f.download(), r) for f, r in zip((s.vx, s.vy, s.vz, s.th), ref[:4])]
+    print("stage", ["%.2e" % e for e in errs])
+    assert max(errs) < 1e-3
