@@ -130,3 +130,63 @@ def test_traffic_table_has_the_stage_kernels():
     t = bench.load_traffic()
     for k in ("fused_vcomp", "fused_vproj", "fused_theta", "x_nonlinear", "z_inverse", "y_inverse", "y_forward"):
         assert t.get(k, 0) > 1e9, k
+
+
+def test_bluestein_half_zero_assumption():
+    """The Bluestein body reads only the first L1/2 rows of each step-A column and forms only the
+    first L1/2 outputs of step A' (fft4.cuh): valid when n <= L2 * (L1/2), for every z length that
+    selects a Bluestein split."""
+    lists = split_lists()
+    seen = set()
+    for n in range(8, 1200):
+        c = choose("z", n, lists)
+        if c is None or not c[2]:
+            continue
+        L, (l1, l2), _ = c
+        assert 2 * n - 1 <= L and n <= l2 * (l1 // 2), (n, L, l1, l2)
+        seen.add(L)
+    assert {1080, 576, 320, 256, 128} <= seen
+
+
+def _c2r_pre_pairs(X, H, nx):
+    """kernels.cuh c2r_pre: Z_k and Z_{H-k} from X_k, X_{H-k} (one (k, H-k) pair per thread)."""
+    Z = np.zeros(H, complex)
+    for k in range(H // 2 + 1):
+        xk, xm = X[k], X[H - k]
+        if k == 0:
+            xk, xm = xk.real + 0j, xm.real + 0j
+        e = xk + np.conj(xm)
+        w = np.exp(2j * np.pi * k / nx)
+        o = (xk - np.conj(xm)) * w
+        Z[k] = complex(e.real - o.imag, e.imag + o.real)
+        if k != 0 and 2 * k != H:
+            Z[H - k] = complex(e.real + o.imag, o.real - e.imag)
+    return Z
+
+
+def _r2c_post_pairs(Z, H, nx):
+    """kernels.cuh r2c_post: X_k and X_{H-k} from Z_k, Z_{H-k}; k = 0 also gives X_H."""
+    X = np.zeros(H + 1, complex)
+    for k in range(H // 2 + 1):
+        zk, zm = Z[k], np.conj(Z[(H - k) % H])
+        e, d = zk + zm, zk - zm
+        t = d * np.exp(-2j * np.pi * k / nx)
+        X[k] = complex(0.5 * (e.real + t.imag), 0.5 * (e.imag - t.real))
+        if 2 * k != H:
+            X[H - k] = complex(0.5 * (e.real - t.imag), -0.5 * (e.imag + t.real))
+    return X
+
+
+@pytest.mark.parametrize("nx", [32, 48, 90, 256, 512])
+def test_real_fft_pair_formulas(nx):
+    """The paired pre-/post-processing of the x pass (a real row of nx points through a complex
+    FFT of H = nx/2 points) against numpy's real transforms."""
+    H = nx // 2
+    rng = np.random.default_rng(nx)
+    x = rng.standard_normal(nx)
+    X = np.fft.rfft(x)                       # half spectrum, H + 1 values
+    z = np.fft.ifft(_c2r_pre_pairs(X, H, nx)) * H  # unnormalised inverse, packed (x_2m, x_2m+1)
+    assert np.allclose(z.real, np.fft.irfft(X, nx)[0::2] * nx, atol=1e-9)
+    assert np.allclose(z.imag, np.fft.irfft(X, nx)[1::2] * nx, atol=1e-9)
+    Zf = np.fft.fft(x[0::2] + 1j * x[1::2])  # forward FFT of the packed row
+    assert np.allclose(_r2c_post_pairs(Zf, H, nx), X, atol=1e-9)
