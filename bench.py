@@ -93,11 +93,12 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def build_solver(api, initial, cfg, precision, fused=True):
+def build_solver(api, initial, cfg, precision, fused=True, nl_fp32=False):
     nz = cfg["nzp"] + cfg["cz"]
     plan = api.Plan((cfg["nx"], cfg["ny"], nz), (0, 0, cfg["cz"]), (0, 0, cfg["oz"]),
                     (cfg["Lx"], cfg["Ly"], cfg["Lz"]), precision=precision)
-    s = api.Solver(plan, api.BOUSS, ord=cfg["ord"], dt=cfg["dt"], nu=cfg["nu"], kappa=cfg["kappa"], fused=fused)
+    s = api.Solver(plan, api.BOUSS, ord=cfg["ord"], dt=cfg["dt"], nu=cfg["nu"], kappa=cfg["kappa"], fused=fused,
+                   nl_fp32=nl_fp32)
     th = initial.convection_theta(plan, seed=cfg["seed"], amp=1e-3)
     fth = initial.to_spectral(plan, [th])[0]
     s.th.copy_from(fth)
@@ -250,7 +251,11 @@ def main():
     ap.add_argument("--caps", default=None, help="Z,Y,X,FUSED,SPLIT: set these instead of autotuning")
     ap.add_argument("--fp64", action="store_true",
                     help="the plain FP64 form instead of FP32-bulk (not the headline: reported against the FP64 peak)")
+    ap.add_argument("--form", default=None, choices=["fp32", "nl32", "fp64"],
+                    help="fp32: FP32-bulk plan; nl32: FP64 state with the nonlinear term in FP32; fp64: plain FP64")
     args = ap.parse_args()
+    if args.form == "fp64":
+        args.fp64 = True
     if args.impl == "reference":
         return run_reference(args)
 
@@ -270,7 +275,9 @@ def main():
     cfg = dict(CFG)
     if args.grid:
         cfg["nx"], cfg["ny"], cfg["nzp"] = (int(v) for v in args.grid.split(","))
-    plan, s = build_solver(api, initial, cfg, api.FP64 if args.fp64 else api.FP32, fused=not args.refseq)
+    nl32 = args.form == "nl32"
+    plan, s = build_solver(api, initial, cfg, api.FP64 if (args.fp64 or nl32) else api.FP32, fused=not args.refseq,
+                           nl_fp32=nl32)
     # tile widths of each kernel family picked by timing RK steps (state restored afterwards)
     if args.fp64:
         caps = None

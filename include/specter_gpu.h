@@ -1,8 +1,8 @@
 /*
  * specter_gpu.h — C ABI of the GB300 (sm_103a) implementation of SPECTER's per-RK-stage hot path.
  *
- * The Fortran driver reaches these entry points through iso_c_binding;
- * each one replaces the reference routine cited beside it (paths inside specter-cfd/SPECTER).
+ * The Fortran driver reaches these entry points through iso_c_binding; each one replaces the
+ * reference routine cited beside it (paths inside specter-cfd/SPECTER).
  *
  * Conventions
  *   - Every function returns an int status: 0 = SPECTER_OK, otherwise one of the codes below;
@@ -32,7 +32,7 @@ enum {
     SPECTER_ERR_CUDA = 5,      /* CUDA runtime error */
     SPECTER_ERR_NONFINITE = 6, /* non-finite value detected in the state */
     SPECTER_ERR_ARG = 7,       /* bad argument (null handle, wrong field kind, ...) */
-    SPECTER_ERR_TIMEOUT = 8,   /* a bounded device wait gave up */
+    /* 8 is unused (no entry point waits with a time limit) */
     SPECTER_ERR_STATE = 9      /* handle used with a different plan / precision */
 };
 
@@ -157,6 +157,11 @@ typedef struct specter_solver_params {
     double v_zend[2];        /* &velbound vxzend, vyzend */
     int fused;               /* 1: fused GB300 stage kernels; 0: the reference call sequence */
     double omega[3];         /* &rotation omegax, omegay, omegaz (SPECTER_ROTBOUSS) */
+    int nl_fp32;             /* the precision form (fused solvers on an FP64 plan; no reference
+                              * counterpart): the nonlinear term -- gradre/advect's transforms and
+                              * products -- in FP32 on an FP32 copy of the state; the state, the
+                              * RK update, the wall round trips with the FC-Gram continuation, the
+                              * projection, fc_filter and all reductions in FP64 */
 } specter_solver_params;
 
 int specter_solver_create(specter_plan *plan, const specter_solver_params *p, specter_solver **out);

@@ -12,7 +12,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libspecter_gpu.so")
 
 OK = 0
-ERR_NAMES = {1: "SHAPE", 2: "TABLE", 3: "BC", 4: "OOM", 5: "CUDA", 6: "NONFINITE", 7: "ARG", 8: "TIMEOUT", 9: "STATE"}
+ERR_NAMES = {1: "SHAPE", 2: "TABLE", 3: "BC", 4: "OOM", 5: "CUDA", 6: "NONFINITE", 7: "ARG", 9: "STATE"}
 
 # every entry point declared in include/specter_gpu.h
 EXPORTS = [
@@ -51,7 +51,7 @@ class SolverParams(C.Structure):
                 ("dt", C.c_double), ("nu", C.c_double), ("kappa", C.c_double),
                 ("gama", C.c_double), ("xmom", C.c_double), ("xtemp", C.c_double),
                 ("v_zsta", C.c_double * 2), ("v_zend", C.c_double * 2), ("fused", C.c_int),
-                ("omega", C.c_double * 3)]
+                ("omega", C.c_double * 3), ("nl_fp32", C.c_int)]
 
 
 _lib = None

@@ -313,10 +313,13 @@ class Solver:
     """The RK loop of src/specter.fpp:1142-1161 with the HD or BOUSS stage body.
 
     solver HD, BOUSS or ROTBOUSS (rotation rate omega).  fused=True runs the GB300 fused stage
-    kernels; fused=False runs the reference's call sequence (gradre, fc_filter, laplak, update, v_imposebc_and_project, ...) on the GPU."""
+    kernels; fused=False runs the reference's call sequence (gradre, fc_filter, laplak, update, v_imposebc_and_project, ...) on the GPU.
+    nl_fp32=True (fused solvers on an FP64 plan) is the precision form: the nonlinear term in FP32,
+    everything that carries the state (update, wall round trips, projection, filter) in FP64."""
 
     def __init__(self, plan: Plan, solver=HD, ord=2, dt=1e-4, nu=1e-3, kappa=0.0, gama=1.0,
-                 xmom=1.0, xtemp=1.0, v_zsta=(0.0, 0.0), v_zend=(0.0, 0.0), fused=True, omega=(0.0, 0.0, 0.0)):
+                 xmom=1.0, xtemp=1.0, v_zsta=(0.0, 0.0), v_zend=(0.0, 0.0), fused=True, omega=(0.0, 0.0, 0.0),
+                 nl_fp32=False):
         self.plan = plan
         p = SolverParams()
         p.solver, p.ord, p.dt, p.nu, p.kappa = solver, ord, dt, nu, kappa
@@ -325,6 +328,7 @@ class Solver:
         p.v_zend[0], p.v_zend[1] = v_zend
         p.fused = 1 if fused else 0
         p.omega[0], p.omega[1], p.omega[2] = omega
+        p.nl_fp32 = 1 if nl_fp32 else 0
         self.params = p
         h = C.c_void_p()
         check(_L(plan).specter_solver_create(plan.h, C.byref(p), C.byref(h)))

@@ -7,6 +7,7 @@
 
 #include "../../include/specter_gpu.h"
 #include "fused.h"
+#include "handles.h"
 #include "ops.h"
 
 using namespace sg;
@@ -15,26 +16,12 @@ namespace sg {
 const char *last_error();
 }
 
-// A plan stays alive while fields or solvers made from it exist: specter_plan_destroy only
-// drops the caller's reference, so handles may be released in any order.
-struct specter_plan {
-    Plan *p;
-    int refs;
-};
-
 static void plan_release(specter_plan *pl) {
     if (--pl->refs == 0) {
         plan_destroy(pl->p);
         delete pl;
     }
 }
-
-struct specter_field {
-    specter_plan *plan;
-    int kind;
-    void *d;
-    size_t bytes;
-};
 
 struct specter_solver {
     specter_plan *plan;
@@ -522,6 +509,13 @@ int specter_solver_create(specter_plan *plan, const specter_solver_params *p, sp
     s->sp.vzend[0] = p->v_zend[0]; s->sp.vzend[1] = p->v_zend[1];
     for (int i = 0; i < 3; i++) s->sp.omega[i] = p->solver == SPECTER_ROTBOUSS ? p->omega[i] : 0.0;
     s->fused = p->fused;
+    s->sp.nl_fp32 = p->nl_fp32 ? 1 : 0;
+    if (s->sp.nl_fp32 && (!p->fused || plan->p->prec != FP64)) {
+        set_error("nl_fp32 needs a fused solver on an FP64 plan");
+        delete s;
+        plan_release(plan);
+        return SPECTER_ERR_ARG;
+    }
     const int nc = p->solver == SPECTER_HD ? 3 : 4;
     int st = SPECTER_OK;
     for (int i = 0; i < 4 && !st; i++) {

@@ -15,6 +15,10 @@ struct FusedState {
     void *E[2] = {nullptr, nullptr};  // z spectra of the unit laplace_z profiles, per column
     void *W[3] = {nullptr, nullptr, nullptr};  // split velocity form: updated components
     int nc = 3;
+    // nl_fp32 (FP64 plans): the FP32 companion plan of the nonlinear term and the FP32 copy of
+    // the stage input it reads
+    Plan *nlp = nullptr;
+    void *v32[4] = {nullptr, nullptr, nullptr, nullptr};
 };
 
 // Unit laplace_z profiles on the physical rows (boundary_mod.fpp:635-675 with c1 = 1, c2 = 0
@@ -41,6 +45,7 @@ __global__ void k_unit_profiles(Geo g, double2 *p1, double2 *p2) {
     }
 }
 
+// FP32 copy of an FP64 field (the nonlinear term's input in the nl_fp32 form)
 __global__ void k_narrow(const double2 *src, float2 *dst, size_t n) {
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
         dst[q] = make_float2((float)src[q].x, (float)src[q].y);
@@ -110,6 +115,28 @@ int fused_create(Plan &P, const StageParams &sp, FusedState **out) {
     if (sp.solver == 1) ok = ok && cudaMalloc(&fs->side, 2 * (size_t)P.ny * P.nzp * P.elt()) == cudaSuccess;  // BOUSS only
     for (int i = 0; i < 2; i++) ok = ok && cudaMalloc(&fs->E[i], P.field_bytes()) == cudaSuccess;
     for (int i = 0; i < 3; i++) ok = ok && cudaMalloc(&fs->W[i], P.field_bytes()) == cudaSuccess;
+    if (ok && sp.nl_fp32) {
+        if (P.prec != FP64) {
+            fused_destroy(fs);
+            set_error("nl_fp32 needs an FP64 plan");
+            return ERR_ARG;
+        }
+        const int n[3] = {P.nx, P.ny, P.nz}, c[3] = {0, 0, P.cz}, o[3] = {0, 0, P.oz};
+        const double len[3] = {P.Lx, P.Ly, P.Lz};
+        const int st = plan_create(&fs->nlp, n, c, o, len, P.tdir.c_str(), FP32);
+        if (st) {
+            fs->nlp = nullptr;
+            fused_destroy(fs);
+            return st;
+        }
+        // the companion runs on the owner's stream, so its launches are ordered with the FP64
+        // column kernels, captured with them and profiled with them
+        cudaStreamSynchronize(fs->nlp->stream);
+        cudaStreamDestroy(fs->nlp->stream);
+        fs->nlp->stream = P.stream;
+        fs->nlp->owner = &P;
+        for (int i = 0; i < fs->nc; i++) ok = ok && cudaMalloc(&fs->v32[i], fs->nlp->field_bytes()) == cudaSuccess;
+    }
     if (!ok) {
         cudaGetLastError();
         fused_destroy(fs);
@@ -132,6 +159,10 @@ unsigned long long fused_bytes(const Plan &P, const FusedState *fs) {
     b += fs->side ? 2ull * P.ny * P.nzp * P.elt() : 0;
     b += (fs->E[0] ? P.field_bytes() : 0) + (fs->E[1] ? P.field_bytes() : 0);
     for (int i = 0; i < 3; i++) b += fs->W[i] ? P.field_bytes() : 0;
+    if (fs->nlp) {
+        b += plan_bytes(*fs->nlp);
+        for (int i = 0; i < 4; i++) b += fs->v32[i] ? fs->nlp->field_bytes() : 0;
+    }
     return b;
 }
 
@@ -146,6 +177,9 @@ void fused_destroy(FusedState *fs) {
         if (fs->E[i]) cudaFree(fs->E[i]);
     for (int i = 0; i < 3; i++)
         if (fs->W[i]) cudaFree(fs->W[i]);
+    for (int i = 0; i < 4; i++)
+        if (fs->v32[i]) cudaFree(fs->v32[i]);
+    if (fs->nlp) plan_destroy(fs->nlp);
     delete fs;
 }
 
@@ -162,10 +196,33 @@ static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], c
     const StageParams &sp = fs->sp;
     const bool bouss = sp.solver >= 1, rot = sp.solver == 2;
     const void *nl[4] = {nullptr, nullptr, nullptr, nullptr};
-    const void *v3[3] = {vin[0], vin[1], vin[2]};
-    int st = Ops<T>::nonlinear(P, v3, bouss ? vin[3] : nullptr, nullptr, 0, bouss ? 4 : 3, nl);
+    int st = OK;
+    if (fs->nlp) {
+        // nl_fp32: the nonlinear term in FP32 from an FP32 copy of the stage input
+        Plan &Q = *fs->nlp;
+        for (int k = 0; k < 3; k++) Q.tile_cap[k] = P.tile_cap[k];  // the autotuned z, y, x caps
+        const size_t n = P.field_elems();
+        for (int i = 0; i < fs->nc; i++) {
+            Launch L_(P, "narrow_state", 24.0 * n);
+            k_narrow<<<152 * 8, 256, 0, P.stream>>>((const double2 *)vin[i], (float2 *)fs->v32[i], n);
+        }
+        if ((st = check_launch("narrow_state"))) return st;
+        const void *v3[3] = {fs->v32[0], fs->v32[1], fs->v32[2]};
+        // the FP32 pipeline finishes the nonlinear term with its forward z transform (with
+        // continuation): the FP64 column kernels read spectra and transform only the state
+        void *spec[4] = {nullptr, nullptr, nullptr, nullptr};
+        for (int c = 0; c < fs->nc; c++)
+            if (!(spec[c] = Q.scratch_field(16 + c))) { set_error("out of device memory (NL spectra)"); return ERR_OOM; }
+        st = Ops<float>::nonlinear(Q, v3, bouss ? fs->v32[3] : nullptr, spec, 0, bouss ? 4 : 3, nullptr);
+        for (int c = 0; c < 4; c++) nl[c] = spec[c];
+    } else {
+        const void *v3[3] = {vin[0], vin[1], vin[2]};
+        st = Ops<T>::nonlinear(P, v3, bouss ? vin[3] : nullptr, nullptr, 0, bouss ? 4 : 3, nl);
+    }
     if (st) return st;
     FusedArgs a{};
+    a.nl32 = fs->nlp ? 1 : 0;
+    a.nl_spec = a.nl32;
     for (int i = 0; i < 4; i++) {
         a.nl[i] = nl[i];
         a.vin[i] = vin[i];
@@ -187,13 +244,16 @@ static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], c
     a.rot = rot ? 1 : 0;
     for (int i = 0; i < 3; i++) a.omega[i] = sp.omega[i];
     const double row = (double)P.ny * P.nxh * P.elt();
+    // NL rows read per column, in units of plan-precision rows: mixed-domain physical rows, or
+    // (nl_fp32) FP32 spectra of all nz rows
+    const double nlr = fs->nlp ? 0.5 * P.nz : (double)P.nzp;
     // reads: NL (physical rows), vin, cold (+ theta for buoyancy), the two unit-profile
     // spectra; writes: vout and pr rows
-    const double bv = row * (3.0 * P.nzp + (6.0 + (bouss ? 1 : 0) + 2.0) * P.nz + 3.0 * P.nz + P.nzp);
+    const double bv = row * (3.0 * nlr + (6.0 + (bouss ? 1 : 0) + 2.0) * P.nz + 3.0 * P.nz + P.nzp);
     if (P.velocity_split) {
         // part 1: NL, vin, cold (+ theta) in, the three updated components out; part 2: those
         // and the unit-profile spectra in, vout and pr rows out
-        const double bc = row * (3.0 * P.nzp + (6.0 + (bouss ? 1 : 0)) * P.nz + 3.0 * P.nz);
+        const double bc = row * (3.0 * nlr + (6.0 + (bouss ? 1 : 0)) * P.nz + 3.0 * P.nz);
         const double bp = row * ((3.0 + 2.0) * P.nz + 3.0 * P.nz + P.nzp);
         if ((st = launch<T>(P, a, kFusedVComp, bc))) return st;
         if ((st = launch<T>(P, a, kFusedVProj, bp))) return st;
@@ -201,7 +261,7 @@ static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], c
         return st;
     }
     if (bouss) {
-        const double bt = row * (1.0 * P.nzp + 3.0 * P.nz + 1.0 * P.nz);
+        const double bt = row * (1.0 * nlr + 3.0 * P.nz + 1.0 * P.nz);
         if ((st = launch<T>(P, a, kFusedTheta, bt))) return st;
         if (!rot && (st = launch<T>(P, a, kFusedHerm, 4.0 * P.ny * P.nz * P.elt()))) return st;
     }

@@ -38,6 +38,9 @@ struct FusedArgs {
     double omega[3];      // rotation rate (rot != 0)
     int bouss;
     int rot;              // ROTBOUSS: Coriolis term, no final theta filter / round trip
+    int nl32;             // the NL fields are FP32 (nl_fp32 form) while the kernel runs in FP64
+    int nl_spec;          // (with nl32) the NL fields are already z spectra: rows [0, nz), the
+                          // forward transform with continuation done by the FP32 pipeline
     float f_dt, f_nu, f_kappa, f_rmp, f_xmom, f_xtemp, f_wall_tmp, f_omega[3];  // FP32 mirrors
     FusedArgs prepared() const {
         FusedArgs b = *this;
@@ -92,6 +95,51 @@ __device__ __forceinline__ void lap_coef_neumann(const Geo &g, int kx, int ky, d
 template <typename T>
 __device__ __forceinline__ double2 d2(C2<T> v) { return make_double2((double)v.x, (double)v.y); }
 
+// Tile of NL_c (rows [0, rows), columns col0 + [0, TK)): by asynchronous copies when the NL field
+// has the kernel's precision, else (FP32 NL fields in an FP64 kernel, the nl_fp32 form) by
+// converting loads, complete for the calling thread on return.  Either way one copy group is
+// committed, so the callers' async_wait_n counts hold.
+template <typename T>
+__device__ __forceinline__ void nl_tile_load(C2<T> *dst, const FusedArgs &a, int c, unsigned col0, unsigned zs, int rows,
+                                             int TK, int nv) {
+    if constexpr (sizeof(T) == 8) {
+        if (a.nl32) {
+            const float2 *src = (const float2 *)a.nl[c] + col0;
+            const int lgTK = lg2(TK);
+            for (int idx = threadIdx.x; idx < rows * TK; idx += blockDim.x) {
+                const int k = idx >> lgTK, cc = idx & (TK - 1);
+                double2 v = make_double2(0.0, 0.0);
+                if (cc < nv) {
+                    const float2 f = __ldg(src + ((unsigned)k * zs + (unsigned)cc));
+                    v = make_double2((double)f.x, (double)f.y);
+                }
+                dst[idx] = v;
+            }
+            async_commit();
+            return;
+        }
+    }
+    tile_load_async(dst, (const C2<T> *)a.nl[c] + col0, zs, rows, TK, nv);
+}
+
+// Rows of the NL tile to load: the mixed-domain physical rows, or every row of a spectrum.
+__device__ __forceinline__ int nl_rows(const Geo &g, const FusedArgs &a) { return a.nl_spec ? g.nz : g.nzp; }
+
+// NL forward z transform with FC-Gram continuation of the tile in X (rows [0, nzp) loaded); with
+// a.nl_spec the tile already holds the spectrum in natural order (FP64 kernels only, whose
+// generic engine keeps natural order: E::pos(k) = k).  Returns the buffer holding the spectrum.
+template <typename T, class E>
+__device__ __forceinline__ C2<T> *nl_forward(const Geo &g, const typename E::Desc &fd, const FusedArgs &a, C2<T> *X,
+                                             C2<T> *Y, int TK) {
+    __syncthreads();
+    if constexpr (sizeof(T) == 8) {
+        if (a.nl_spec) return X;
+    }
+    fc_continuation<T>(g, X, TK);
+    __syncthreads();
+    return E::run(X, Y, TK, fd, -1);
+}
+
 // ----------------------------------------------------------------------------------------------
 // velocity: device functions shared by the one-block-per-tile kernel (k_fused_velocity) and the
 // split pair (k_fused_vcomp per component, k_fused_vproj for the projection)
@@ -129,10 +177,7 @@ __device__ void vel_update(const Geo &g, const typename E::Desc &fd, const Fused
     const bool stage2 = (size_t)E::kBuffers * fd.L >= 2 * (size_t)nz;  // vin and cold both fit in X
     const T dt = pick<T>(a.dt, a.f_dt), nu = pick<T>(a.nu, a.f_nu), rmp = pick<T>(a.rmp, a.f_rmp);
     const T xmom = pick<T>(a.xmom, a.f_xmom);
-    __syncthreads();
-    fc_continuation<T>(g, X, TK);
-    __syncthreads();
-    V *R = E::run(X, Y, TK, fd, -1);
+    V *R = nl_forward<T, E>(g, fd, a, X, Y, TK);
     if (buoy) {
         async_wait();
         __syncthreads();
@@ -395,15 +440,15 @@ __global__ void __launch_bounds__(E::kWideThreads, 1) k_fused_velocity(Geo g, ty
         V *Uc = U + c3 * tile;
         const bool buoy = c3 == 2 && a.bouss;
         if (c3 == 0) {
-            tile_load_async(X, (const V *)a.nl[0] + t.col0, t.zs, nzp, TK, t.nv);
-            tile_load_async(U + tile, (const V *)a.nl[1] + t.col0, t.zs, nzp, TK, t.nv);
+            nl_tile_load<T>(X, a, 0, t.col0, t.zs, nl_rows(g, a), TK, t.nv);
+            nl_tile_load<T>(U + tile, a, 1, t.col0, t.zs, nl_rows(g, a), TK, t.nv);
             async_wait_n<1>();
         } else {
             async_wait();
             __syncthreads();
-            for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) X[idx] = Uc[idx];
+            for (int idx = threadIdx.x; idx < nl_rows(g, a) * TK; idx += blockDim.x) X[idx] = Uc[idx];
             __syncthreads();
-            if (c3 == 1) tile_load_async(U + 2 * tile, (const V *)a.nl[2] + t.col0, t.zs, nzp, TK, t.nv);
+            if (c3 == 1) nl_tile_load<T>(U + 2 * tile, a, 2, t.col0, t.zs, nl_rows(g, a), TK, t.nv);
             else if (buoy) tile_load_async(Uc, (const V *)a.vin[3] + t.col0, t.zs, nz, TK, t.nv);
         }
         vel_update<T, E>(g, fd, a, t, c3, Uc, X, Y, buoy);
@@ -427,7 +472,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_vcomp(Geo g, 
     V *X = Uc + (size_t)nz * TK;
     V *Y = X + (size_t)fd.L * TK;
     const bool buoy = c3 == 2 && a.bouss;
-    tile_load_async(X, (const V *)a.nl[c3] + t.col0, t.zs, nzp, TK, t.nv);
+    nl_tile_load<T>(X, a, c3, t.col0, t.zs, nl_rows(g, a), TK, t.nv);
     if (buoy) {
         tile_load_async(Uc, (const V *)a.vin[3] + t.col0, t.zs, nz, TK, t.nv);
         async_wait_n<1>();
@@ -492,13 +537,10 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
         const int tile = nz * TK;
         const size_t zs = (size_t)g.ny * g.ldx, col0 = (size_t)ky * g.ldx + kx0;
         const bool stage2 = (size_t)E::kBuffers * L >= 2 * (size_t)nz;
-        tile_load_async(X, (const V *)a.nl[3] + col0, zs, nzp, TK, nv);
+        nl_tile_load<T>(X, a, 3, (unsigned)col0, (unsigned)zs, nl_rows(g, a), TK, nv);
         tile_load_async(Th, (const V *)a.vin[2] + col0, zs, nz, TK, nv);
         async_wait_n<1>();
-        __syncthreads();
-        fc_continuation<T>(g, X, TK);
-        __syncthreads();
-        V *R = E::run(X, Y, TK, fd, -1);
+        V *R = nl_forward<T, E>(g, fd, a, X, Y, TK);
         async_wait();
         __syncthreads();
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {

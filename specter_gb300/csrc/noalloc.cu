@@ -16,12 +16,18 @@
 //     threads) race on it and must be serialised by the caller.  Each call writes every slot it
 //     reads afterwards, and clears the two result slots before use.
 //   - the first call on a device looks up the array's device address (cudaGetSymbolAddress) with
-//     that device current; make that first call before any stream capture.
+//     that device current and keeps it for later calls; make that first call before any stream
+//     capture.  The lookup is guarded by a mutex, so first calls from several host threads are
+//     safe.  cudaDeviceReset unloads the module and leaves the kept address stale: a process that
+//     resets a device must not call this entry point on that device afterwards.
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "../../include/specter_gpu.h"
+#include "handles.h"
 #include "kernels_elem.cuh"
+#include "ops.h"
 
 namespace sg {
 
@@ -48,16 +54,22 @@ static __global__ void k_wall_finish(const double *partial, int nblocks, double 
 }
 
 // device address of g_wall_scratch for each device, looked up once with that device current
+static std::mutex g_addr_mutex;
+static double *g_addr[64] = {nullptr};
+
 static double *scratch_address() {
-    static double *addr[64] = {nullptr};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-    if (!addr[dev]) {
+    std::lock_guard<std::mutex> lock(g_addr_mutex);
+    if (!g_addr[dev]) {
         double *p = nullptr;
-        if (cudaGetSymbolAddress((void **)&p, g_wall_scratch) != cudaSuccess) return nullptr;
-        addr[dev] = p;
+        if (cudaGetSymbolAddress((void **)&p, g_wall_scratch) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        g_addr[dev] = p;
     }
-    return addr[dev];
+    return g_addr[dev];
 }
 
 template <typename T>
@@ -67,12 +79,20 @@ static int wall_check_static(Plan &P, const void *a, const void *b, double *bot,
     double2 *bcA = (double2 *)base, *bcB = bcA + kWallSlots;
     double *partial = base + 2 * 2 * kWallSlots, *result = partial + 2 * kStaticBlocks;
     const double2 *wtw = (const double2 *)P.dwtw;
-    cudaMemsetAsync(result, 0, 2 * sizeof(double), P.stream);
-    k_wall_eval<T><<<dim3(cdiv(P.nxh, 64), P.ny), 64, 0, P.stream>>>(P.geo, (const C2<T> *)a, 1.0, wtw, bcA, 0);
-    if (b) k_wall_eval<T><<<dim3(cdiv(P.nxh, 64), P.ny), 64, 0, P.stream>>>(P.geo, (const C2<T> *)b, 1.0, wtw, bcB, 0);
-    k_reduce_walls<<<kStaticBlocks, kThreads, 0, P.stream>>>(P.geo, bcA, b ? bcB : nullptr, partial);
+    const dim3 grid(cdiv(P.nxh, 64), P.ny);
+    const double col = (double)P.nz * P.ny * P.nxh * (double)P.elt();  // one field read
+    if (cudaMemsetAsync(result, 0, 2 * sizeof(double), P.stream) != cudaSuccess) return check_launch("bouncheck_z_static clear");
+    { Launch L_(P, "wall_eval", col); k_wall_eval<T><<<grid, 64, 0, P.stream>>>(P.geo, (const C2<T> *)a, 1.0, wtw, bcA, 0); }
+    if (int st = check_launch("bouncheck_z_static wall_eval")) return st;
+    if (b) {
+        { Launch L_(P, "wall_eval", col); k_wall_eval<T><<<grid, 64, 0, P.stream>>>(P.geo, (const C2<T> *)b, 1.0, wtw, bcB, 0); }
+        if (int st = check_launch("bouncheck_z_static wall_eval")) return st;
+    }
+    { Launch L_(P, "reduce_walls", 64.0 * P.nxh * P.ny); k_reduce_walls<<<kStaticBlocks, kThreads, 0, P.stream>>>(P.geo, bcA, b ? bcB : nullptr, partial); }
+    if (int st = check_launch("bouncheck_z_static reduce_walls")) return st;
     const double inv = 1.0 / (double)((long long)P.nx * P.ny * P.nz);
-    k_wall_finish<<<1, 32, 0, P.stream>>>(partial, kStaticBlocks, inv, result);
+    { Launch L_(P, "wall_finish", 16.0 * kStaticBlocks); k_wall_finish<<<1, 32, 0, P.stream>>>(partial, kStaticBlocks, inv, result); }
+    if (int st = check_launch("bouncheck_z_static wall_finish")) return st;
     double host[2];
     if (cudaMemcpyAsync(host, result, sizeof host, cudaMemcpyDeviceToHost, P.stream) != cudaSuccess ||
         cudaStreamSynchronize(P.stream) != cudaSuccess) {
@@ -85,18 +105,6 @@ static int wall_check_static(Plan &P, const void *a, const void *b, double *bot,
 }
 
 }  // namespace sg
-
-// handle layout: identical to the definitions in capi.cu, which creates these handles
-struct specter_plan {
-    sg::Plan *p;
-    int refs;
-};
-struct specter_field {
-    specter_plan *plan;
-    int kind;
-    void *d;
-    size_t bytes;
-};
 
 extern "C" int specter_bouncheck_z_static(specter_plan *plan, const specter_field *a, const specter_field *b,
                                           double *bot, double *top) {

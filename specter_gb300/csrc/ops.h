@@ -12,6 +12,10 @@ struct StageParams {
     double dt, nu, kappa, xmom, xtemp;  // xmom, xtemp already multiplied by gama
     double vzsta[2], vzend[2];
     double omega[3];  // rotation rate (ROTBOUSS)
+    // 1 on an FP64 plan: the nonlinear term runs in FP32 (on an FP32 copy of the state, through
+    // a companion FP32 plan); the state, the RK update, the wall round trips, the projection, the
+    // filter and the reductions stay FP64
+    int nl_fp32;
 };
 
 template <typename T> struct Ops {

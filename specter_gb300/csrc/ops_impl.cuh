@@ -52,15 +52,8 @@ static int elem_blocks(const Plan &P, int rows) {
     return (int)(b < 1 ? 1 : b);
 }
 
-// Brackets one kernel launch for the plan's launch counter and (when enabled) its event
-// profiler.  `bytes` is the launch's algorithmic traffic: each input element read once and
-// each output element written once.
-struct Launch {
-    Plan &P;
-    Launch(Plan &p, const char *name, double bytes) : P(p) { P.prof_begin(name, bytes); }
-    ~Launch() { P.prof_end(); }
-};
-
+// Launch (plan.h) brackets each kernel launch; `bytes` is the launch's algorithmic traffic:
+// each input element read once and each output element written once.
 static double cplx_rows(const Plan &P, double rows) { return rows * P.ny * P.nxh * (double)P.elt(); }
 
 // ------------------------------------------------------------------------- launchers

@@ -220,7 +220,8 @@ int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], cons
         delete p;
         return ERR_SHAPE;
     }
-    int st = load_tables(p, tdir ? tdir : ".");
+    p->tdir = tdir ? tdir : ".";
+    int st = load_tables(p, p->tdir.c_str());
     if (st) { delete p; return st; }
     // grids and wavenumbers, src/specter.fpp:683-800
     const double pi = 3.14159265358979323846;
@@ -355,6 +356,7 @@ static cudaEvent_t take_event(Plan *p) {
 }
 
 void Plan::prof_begin(const char *name, double bytes) {
+    if (owner) { owner->prof_begin(name, bytes); return; }
     launches++;
     if (!profile) return;
     Rec r{name, bytes, take_event(this), take_event(this)};
@@ -363,6 +365,7 @@ void Plan::prof_begin(const char *name, double bytes) {
 }
 
 void Plan::prof_end() {
+    if (owner) { owner->prof_end(); return; }
     if (!profile || recs.empty()) return;
     cudaEventRecord(recs.back().b, stream);
     if (recs.size() >= 4096) prof_flush();
@@ -404,7 +407,7 @@ void plan_destroy(Plan *p) {
     if (p->copy_stream) { cudaStreamSynchronize(p->copy_stream); cudaStreamDestroy(p->copy_stream); }
     for (cudaEvent_t e : p->xfer_ev)
         if (e) cudaEventDestroy(e);
-    if (p->stream) cudaStreamDestroy(p->stream);
+    if (p->stream && !p->owner) cudaStreamDestroy(p->stream);  // a companion borrows its owner's
     delete p;
 }
 

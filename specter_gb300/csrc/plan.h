@@ -15,7 +15,7 @@ enum Prec { FP64 = 0, FP32 = 1 };
 // error status shared with the C-ABI (include/specter_gpu.h)
 enum Status {
     OK = 0, ERR_SHAPE = 1, ERR_TABLE = 2, ERR_BC = 3, ERR_OOM = 4, ERR_CUDA = 5,
-    ERR_NONFINITE = 6, ERR_ARG = 7, ERR_TIMEOUT = 8, ERR_STATE = 9
+    ERR_NONFINITE = 6, ERR_ARG = 7, ERR_STATE = 9
 };
 
 void set_error(const std::string &msg);
@@ -64,6 +64,10 @@ struct Geo {
 
 struct Plan {
     Prec prec = FP64;
+    std::string tdir;         // FC-Gram table directory the plan was built from
+    // A companion plan (the FP32 plan of the nonlinear term of a mixed-precision solver) runs on
+    // its owner's stream and counts and profiles its launches in its owner's records.
+    Plan *owner = nullptr;
     int nx = 0, ny = 0, nz = 0, cz = 0, oz = 0, nxh = 0, nzp = 0, ldx = 0, H = 0;
     double Lx = 1, Ly = 1, Lz = 1, Dkx = 1, Dky = 1, Dkz = 1, dz = 1;
     std::vector<double> kx, ky, kz, z, dir, fx, fy, fz;
@@ -114,6 +118,14 @@ struct Plan {
     size_t field_bytes() const { return field_elems() * elt(); }
     size_t real_elems() const { return (size_t)nz * ny * nx; }
     void *scratch_field(int i);
+};
+
+// Brackets one kernel launch: counts it and, with profiling on, records CUDA events around it
+// attributed to `name` with `bytes` algorithmic bytes.
+struct Launch {
+    Plan &P;
+    Launch(Plan &p, const char *name, double bytes) : P(p) { P.prof_begin(name, bytes); }
+    ~Launch() { P.prof_end(); }
 };
 
 int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], const double len[3],

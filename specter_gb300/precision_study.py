@@ -1,4 +1,9 @@
-"""FP32-bulk precision form against the plain FP64 form, both on the GPU.
+"""A precision form against the plain FP64 form, both on the GPU.
+
+Forms: nl32 (default) keeps the state and everything that carries it through a z transform in
+FP64 and runs the nonlinear term in FP32 (Solver(..., nl_fp32=True) on an FP64 plan); fp32 is
+the FP32-bulk plan (every transform FP32, FP64 only for the continuation arithmetic, the wall
+solve and the reductions).
 
 The same seeded case runs through both forms; at each checkpoint the relative L2 error of every
 state field is reported on the physical grid (rows z < nzp):
@@ -11,7 +16,7 @@ CPU restatement of the reference to 1e-10 (tests/test_gpu_configs.py), so this i
 form's error against the reference algorithm.
 
     python -m specter_gb300.precision_study --case channel256 --check 100,1000
-    python -m specter_gb300.precision_study --case bouss512 --check 10,100,1000
+    python -m specter_gb300.precision_study --case bouss512 --check 10,100,1000 [--form fp32]
 
 Cases (seeded initial fields of specter_gb300.initial):
   channel64   HD channel 64^2 x 65 (+25), Lz = 2, RK2, dt 1e-4, nu 1e-3, |k| <= 8, amp 0.05
@@ -38,12 +43,12 @@ CASES = {
 SEED = 20261203
 
 
-def make_solver(api, initial, c, precision, fused=True):
+def make_solver(api, initial, c, precision, fused=True, nl_fp32=False):
     nz = c["nzp"] + 25
     plan = api.Plan((c["nx"], c["ny"], nz), (0, 0, 25), (0, 0, 5), (1.0, 1.0, c["Lz"]), precision=precision)
     bouss = c["solver"] == "BOUSS"
     s = api.Solver(plan, api.BOUSS if bouss else api.HD, ord=c["ord"], dt=c["dt"], nu=c["nu"],
-                   kappa=c["kappa"], fused=fused)
+                   kappa=c["kappa"], fused=fused, nl_fp32=nl_fp32)
     if bouss:
         th = initial.convection_theta(plan, seed=SEED, amp=c["amp"])
         s.th.copy_from(initial.to_spectral(plan, [th])[0])
@@ -85,11 +90,16 @@ def main(argv=None):
     ap.add_argument("--case", default="channel256", choices=sorted(CASES))
     ap.add_argument("--check", default="100,1000", help="comma-separated step counts")
     ap.add_argument("--fused", type=int, default=1)
+    ap.add_argument("--form", default="nl32", choices=["nl32", "fp32"],
+                    help="nl32: FP64 state, FP32 nonlinear term (nl_fp32); fp32: the FP32-bulk plan")
     args = ap.parse_args(argv)
     from specter_gb300 import api, initial
     c = CASES[args.case]
     checks = sorted({int(x) for x in args.check.split(",")})
-    p32, s32 = make_solver(api, initial, c, api.FP32, bool(args.fused))
+    if args.form == "nl32":
+        p32, s32 = make_solver(api, initial, c, api.FP64, True, nl_fp32=True)
+    else:
+        p32, s32 = make_solver(api, initial, c, api.FP32, bool(args.fused))
     p64, s64 = make_solver(api, initial, c, api.FP64, bool(args.fused))
     names = ["vx", "vy", "vz"] + (["th"] if c["solver"] == "BOUSS" else [])
     scratch = (p64.field(api.COMPLEX), p64.field(api.REAL))
@@ -112,8 +122,8 @@ def main(argv=None):
         rows.append({"steps": n, "rel_l2": errs, "max": max(errs[k_] for k_ in names)})
         print(json.dumps({"progress": rows[-1]}), flush=True)
     pts = c["nx"] * c["ny"] * c["nzp"] * c["ord"] * done
-    line = {"case": args.case, "config": c, "seed": SEED, "fused": bool(args.fused), "checkpoints": rows,
-            "fp32_mpts_stages_per_s": round(pts / t32 / 1e6, 2), "fp64_mpts_stages_per_s": round(pts / t64 / 1e6, 2),
+    line = {"case": args.case, "form": args.form, "config": c, "seed": SEED, "fused": bool(args.fused), "checkpoints": rows,
+            "form_mpts_stages_per_s": round(pts / t32 / 1e6, 2), "fp64_mpts_stages_per_s": round(pts / t64 / 1e6, 2),
             "metric": "relative L2 on physical rows; pr in the mixed domain"}
     print(json.dumps(line), flush=True)
     return line

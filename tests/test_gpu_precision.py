@@ -1,0 +1,106 @@
+"""The precision form (nl_fp32: FP64 state, FP32 nonlinear term) and the plain FP64 form at the
+headline z length (nz = 513 physical + 25 continuation = 538 = 2*269, Bluestein), through the C
+ABI, against the FP64 oracle.
+
+Why this split of precisions: the FC-Gram continuation multiplies rounding in the 2d
+wall-adjacent rows by up to sum|dir| = 9.5e3, and every operation that carries the state through
+a z transform (the wall round trips of v_imposebc_and_project and s_imposebc, the projection,
+fc_filter of theta and its c2r/r2c round trip) feeds those rows.  In FP32 each of them alone
+costs 1e-5..4e-4 relative error after 100 Rayleigh-Benard steps.  The nonlinear term enters the
+state multiplied by dt, so its FP32 rounding stays below the gate: the form keeps the nonlinear
+term (its transforms and products) in FP32 and everything else in FP64.
+
+Rayleigh-Benard grid 32 x 32 x 513 (+25): cfg3's z grid and physics (Lz = 1, nu = kappa = 1e-4,
+dt = 1e-5, RK2, theta' = 1e-3 U(-1,1) z(1-z), v = 0) on a small periodic plane.
+"""
+import numpy as np
+import pytest
+
+from conftest import make_pair, rel
+
+pytestmark = pytest.mark.gpu
+
+STEPS = 20
+SEED = 20261203
+
+
+@pytest.fixture(scope="module")
+def convection():
+    from specter_gb300 import api, initial
+    plan, g = make_pair(32, 32, 513, 1.0)
+    th = initial.convection_theta(plan, seed=SEED, amp=1e-3)
+    th0 = g.fftp3d_real_to_complex(th)
+    zero = np.zeros(g.sshape, complex)
+    kw = dict(dt=1e-5, nu=1e-4, kappa=1e-4, ord=2)
+    p = g.params(**kw)
+    ref = g.run(p, STEPS, zero, zero, zero, zero, th=th0)
+
+    def run(**opts):
+        s = api.Solver(plan, api.BOUSS, **kw, **opts)
+        for f, a in zip((s.vx, s.vy, s.vz, s.th, s.pr), (zero, zero, zero, th0, zero)):
+            f.upload(a)
+        s.step(STEPS)
+        out = [f.download() for f in (s.vx, s.vy, s.vz, s.th, s.pr)]
+        s.close()
+        return out
+
+    return plan, g, ref, run
+
+
+def _errors(g, got, ref):
+    """relative L2 on the physical grid (c2r of both spectra, rows z < nzp)"""
+    nzp = g.nz - g.cz
+    out = []
+    for a, b in zip(got[:4], [ref[0], ref[1], ref[2], ref[3]]):
+        ra, rb = g.fftp3d_complex_to_real(a)[:nzp], g.fftp3d_complex_to_real(b)[:nzp]
+        out.append(rel(ra, rb))
+    return out
+
+
+def test_fp64_bouss_nz538(convection):
+    """Plain FP64, fused and reference call sequence, at NZ = 538."""
+    plan, g, ref, run = convection
+    for fused in (True, False):
+        got = run(fused=fused)
+        for a, b in zip(got[:4], ref[:4]):
+            assert rel(a, b) < 1e-11, fused
+        assert rel(got[4][..., : g.nz - g.cz], ref[4][..., : g.nz - g.cz]) < 1e-8, fused
+
+
+def test_nl_fp32_bouss_nz538(convection):
+    """The precision form after 20 steps: theta (which the FP32 nonlinear term reaches only
+    through v.grad theta with v ~ 1e-8) to 1e-9, the velocity (driven by buoyancy from rest, so
+    its error is relative to a small field) to 5e-6."""
+    plan, g, ref, run = convection
+    got = run(fused=True, nl_fp32=True)
+    e = _errors(g, got, ref)
+    print("nl_fp32 vs oracle after %d steps: vx %.2e vy %.2e vz %.2e th %.2e" % (STEPS, *e))
+    assert max(e[:3]) < 5e-6
+    assert e[3] < 1e-9
+
+
+def test_nl_fp32_channel():
+    """The plain channel configuration (64 x 64 x 65, 100 RK2 steps) in the precision form."""
+    from specter_gb300 import api, initial
+    plan, g = make_pair(64, 64, 65, 2.0)
+    real = initial.channel_velocity(plan, seed=SEED, amp=0.05, kmax=8)
+    v0 = [g.fftp3d_real_to_complex(r) for r in real]
+    pr0 = np.zeros(g.sshape, complex)
+    kw = dict(dt=1e-4, nu=1e-3, ord=2)
+    ref = g.run(g.params(**kw), 100, *v0, pr0)
+    s = api.Solver(plan, api.HD, fused=True, nl_fp32=True, **kw)
+    for f, a in zip((s.vx, s.vy, s.vz, s.pr), v0 + [pr0]):
+        f.upload(a)
+    s.step(100)
+    got = [f.download() for f in (s.vx, s.vy, s.vz)]
+    e = [rel(a, b) for a, b in zip(got, ref[:3])]
+    print("nl_fp32 channel vs oracle after 100 steps: %.2e %.2e %.2e" % tuple(e))
+    assert max(e) < 1e-5
+
+
+def test_nl_fp32_needs_fp64_plan():
+    from specter_gb300 import api, SpecterError
+    plan = api.Plan((16, 16, 58), (0, 0, 25), (0, 0, 5), (1.0, 1.0, 2.0), precision=api.FP32)
+    with pytest.raises(SpecterError) as e:
+        api.Solver(plan, api.HD, fused=True, nl_fp32=True)
+    assert e.value.code == 7

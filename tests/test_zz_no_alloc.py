@@ -4,10 +4,13 @@ Some callers may not allocate device memory once they run (a serving loop that h
 its memory budget, code inside the RK loop that cannot take the synchronisation of
 cudaMalloc/cudaFree).  This entry point keeps its working memory in one fixed device array;
 here it must reproduce specter_bouncheck_z through the C ABI on consecutive calls (the array
-keeps the previous call's contents) and reject grids larger than the array.
+keeps the previous call's contents), allocate nothing on a fresh plan, accept the largest grid
+the array holds and reject larger ones.
 """
 import numpy as np
 import pytest
+
+from conftest import make_pair
 
 pytestmark = pytest.mark.gpu
 
@@ -32,6 +35,38 @@ def test_static_matches_allocating(precision):
         one_ref = api.bouncheck_z(plan, fa)
         one_got = api.bouncheck_z_static(plan, fa)
         assert one_got == pytest.approx(one_ref, rel=1e-12, abs=0), call
+
+
+def test_static_allocates_nothing():
+    """On a fresh plan whose scratch was never touched, the static call leaves the device's free
+    memory unchanged (the allocating variant would create its scratch fields here)."""
+    from specter_gb300 import api
+    warm = api.Plan((16, 16, 58), (0, 0, 25), (0, 0, 5), (1.0, 1.0, 2.0), precision=0)
+    api.bouncheck_z_static(warm, warm.field())  # loads the module and looks up the array first
+    plan = api.Plan((32, 24, 58), (0, 0, 25), (0, 0, 5), (1.0, 1.0, 2.0), precision=0)
+    rng = np.random.default_rng(5)
+    fa, fb = _fields(plan, rng)
+    plan.synchronize()
+    free0, _ = api.device_memory()
+    for _ in range(2):
+        api.bouncheck_z_static(plan, fa, fb)
+        api.bouncheck_z_static(plan, fa)
+    plan.synchronize()
+    free1, _ = api.device_memory()
+    assert free1 == free0
+
+
+def test_static_max_columns(oracle_mod):
+    """(nx/2 + 1) * ny = 64 * 1024 = 65536 columns: the largest grid the array holds."""
+    from specter_gb300 import api
+    plan, g = make_pair(126, 1024, 33, 1.0)
+    rng = np.random.default_rng(23)
+    a = (rng.standard_normal(g.sshape) + 1j * rng.standard_normal(g.sshape)) * 1e-2
+    b = (rng.standard_normal(g.sshape) + 1j * rng.standard_normal(g.sshape)) * 1e-2
+    fa, fb = plan.field(data=a), plan.field(data=b)
+    got = api.bouncheck_z_static(plan, fa, fb)
+    assert got == pytest.approx(g.bouncheck_z(a, b), rel=1e-11)
+    assert got == pytest.approx(api.bouncheck_z(plan, fa, fb), rel=1e-12, abs=0)
 
 
 def test_static_rejects_large_grid():
