@@ -585,11 +585,7 @@ int specter_solver_step(specter_solver *s, int nsteps) {
     const int nc = s->sp.solver == SPECTER_HD ? 3 : 4;
     if (s->fused) {
         void *v[4] = {s->v[0]->d, s->v[1]->d, s->v[2]->d, s->v[3] ? s->v[3]->d : nullptr};
-        for (int t = 0; t < nsteps; t++) {
-            int st = fused_step(P, s->fs, v, s->pr->d);
-            if (st) return st;
-        }
-        return SPECTER_OK;
+        return fused_step(P, s->fs, v, s->pr->d, nsteps);
     }
     for (int t = 0; t < nsteps; t++) {
         // rkstep1: C_i = v_i (hd_rkstep1.f90:4-6, bouss_rkstep1.f90:4-7)

@@ -4,12 +4,39 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
+#include "ff.cuh"
+
 namespace sg {
 
 template <typename T> struct cplx_t;
 template <> struct cplx_t<double> { using type = double2; };
 template <> struct cplx_t<float> { using type = float2; };
+template <> struct cplx_t<ff> { using type = ffc; };
 template <typename T> using C2 = typename cplx_t<T>::type;
+
+// the three arithmetic types of the kernels: FP32, FP64 and float-float (ff.cuh)
+template <typename T> constexpr bool is_f32 = std::is_same<T, float>::value;
+template <typename T> constexpr bool is_f64 = std::is_same<T, double>::value;
+template <typename T> constexpr bool is_ff = std::is_same<T, ff>::value;
+
+// read-only global load of a complex element (float-float complex as one 16-byte load)
+template <typename V> __device__ __forceinline__ V ldg_v(const V *p) { return __ldg(p); }
+template <> __device__ __forceinline__ ffc ldg_v<ffc>(const ffc *p) {
+    const float4 f = __ldg((const float4 *)p);
+    ffc r;
+    r.x = ff(f.x, f.y);
+    r.y = ff(f.z, f.w);
+    return r;
+}
+// a complex FP32 value in the kernel's type (exact)
+template <typename T> __device__ __forceinline__ C2<T> from_f2(float2 v) {
+    C2<T> r;
+    r.x = v.x;
+    r.y = v.y;
+    return r;
+}
 
 template <typename T> __host__ __device__ __forceinline__ C2<T> mk(T r, T i) { C2<T> c; c.x = r; c.y = i; return c; }
 template <typename V> __host__ __device__ __forceinline__ V cadd(V a, V b) { a.x += b.x; a.y += b.y; return a; }

@@ -29,7 +29,7 @@ struct FFTDesc {
 
 template <typename T>
 __device__ __forceinline__ C2<T> tw_at(const C2<T> *tw, int t, int sign) {
-    C2<T> w = __ldg(tw + t);
+    C2<T> w = ldg_v(tw + t);
     if (sign > 0) w.y = -w.y;
     return w;
 }
@@ -42,10 +42,11 @@ __device__ __forceinline__ void butterfly(C2<T> *a, int s, const C2<T> *tw, int 
         a[0] = cadd(t, a[1]);
         a[1] = csub(t, a[1]);
     } else if constexpr (R == 3) {
-        const T s3 = (T)s * (T)0.86602540378443864676372317075294;
+        constexpr T k3 = T(0.86602540378443864676372317075294), half = T(0.5);
+        const T s3 = s * k3;
         V t1 = cadd(a[1], a[2]);
         V t2 = cmuli(cscale(csub(a[1], a[2]), s3), 1);
-        V m1 = mk<T>(a[0].x - (T)0.5 * t1.x, a[0].y - (T)0.5 * t1.y);
+        V m1 = mk<T>(a[0].x - half * t1.x, a[0].y - half * t1.y);
         a[0] = cadd(a[0], t1);
         a[1] = cadd(m1, t2);
         a[2] = csub(m1, t2);
@@ -55,8 +56,8 @@ __device__ __forceinline__ void butterfly(C2<T> *a, int s, const C2<T> *tw, int 
         a[0] = cadd(t0, t2); a[2] = csub(t0, t2);
         a[1] = cadd(t1, t3); a[3] = csub(t1, t3);
     } else if constexpr (R == 5) {
-        const T c1 = (T)0.30901699437494742410229341718282, c2 = (T)-0.80901699437494742410229341718282;
-        const T s1 = (T)0.95105651629515357211643933337938, s2 = (T)0.58778525229247312916870595463907;
+        constexpr T c1 = T(0.30901699437494742410229341718282), c2 = T(-0.80901699437494742410229341718282);
+        constexpr T s1 = T(0.95105651629515357211643933337938), s2 = T(0.58778525229247312916870595463907);
         V t1 = cadd(a[1], a[4]), t2 = cadd(a[2], a[3]);
         V t3 = csub(a[1], a[4]), t4 = csub(a[2], a[3]);
         V m1 = mk<T>(a[0].x + c1 * t1.x + c2 * t2.x, a[0].y + c1 * t1.y + c2 * t2.y);
@@ -67,7 +68,7 @@ __device__ __forceinline__ void butterfly(C2<T> *a, int s, const C2<T> *tw, int 
         a[1] = cadd(m1, n1); a[4] = csub(m1, n1);
         a[2] = cadd(m2, n2); a[3] = csub(m2, n2);
     } else if constexpr (R == 8) {
-        const T h = (T)0.70710678118654752440084436210485;
+        constexpr T h = T(0.70710678118654752440084436210485);
         V e[4] = {a[0], a[2], a[4], a[6]}, o[4] = {a[1], a[3], a[5], a[7]};
         butterfly<T, 4>(e, s, tw, LoverR);
         butterfly<T, 4>(o, s, tw, LoverR);
@@ -154,7 +155,7 @@ __device__ __noinline__ C2<T> *fft_exec(C2<T> *X, C2<T> *Y, int B, const FFTDesc
     }
     __syncthreads();
     C2<T> *R = stockham<T>(X, Y, B, d, -1);
-    for (int idx = threadIdx.x; idx < L * B; idx += blockDim.x) R[idx] = cmul(R[idx], __ldg(filt + (idx >> lgB)));
+    for (int idx = threadIdx.x; idx < L * B; idx += blockDim.x) R[idx] = cmul(R[idx], ldg_v(filt + (idx >> lgB)));
     __syncthreads();
     C2<T> *O = (R == X) ? Y : X;
     R = stockham<T>(R, O, B, d, +1);

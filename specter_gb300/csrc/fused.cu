@@ -19,6 +19,13 @@ struct FusedState {
     // the stage input it reads
     Plan *nlp = nullptr;
     void *v32[4] = {nullptr, nullptr, nullptr, nullptr};
+    // the column kernels of that form compute in float-float: their z FFT tables, and the state
+    // (vq, prq) held in float-float inside the RK loop (converted from and to the FP64 fields at
+    // the ends of fused_step / fused_stage; cq: the RK step start for fused_stage)
+    FFTTable tzq;
+    void *vq[4] = {nullptr, nullptr, nullptr, nullptr};
+    void *cq[4] = {nullptr, nullptr, nullptr, nullptr};
+    void *prq = nullptr;
 };
 
 // Unit laplace_z profiles on the physical rows (boundary_mod.fpp:635-675 with c1 = 1, c2 = 0
@@ -45,10 +52,45 @@ __global__ void k_unit_profiles(Geo g, double2 *p1, double2 *p2) {
     }
 }
 
-// FP32 copy of an FP64 field (the nonlinear term's input in the nl_fp32 form)
 __global__ void k_narrow(const double2 *src, float2 *dst, size_t n) {
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x)
         dst[q] = make_float2((float)src[q].x, (float)src[q].y);
+}
+
+// float-float <-> FP64 fields of the nl_fp32 form (in place allowed: both are 16 bytes a
+// complex element).  These conversions run on the FP64 pipe; they happen once per field per
+// fused_step call, not per stage.
+__global__ void k_d2q(const double2 *src, ffc *dst, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const double2 v = src[q];
+        ffc r;
+        r.x = ff_from_double(v.x);
+        r.y = ff_from_double(v.y);
+        dst[q] = r;
+    }
+}
+__global__ void k_q2d(const ffc *src, double2 *dst, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const ffc v = src[q];
+        dst[q] = make_double2(ff_to_double(v.x), ff_to_double(v.y));
+    }
+}
+// FP32 copy of a float-float field (its leading parts): the nonlinear term's input
+__global__ void k_q2f(const ffc *src, float2 *dst, size_t n) {
+    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        const float4 v = *(const float4 *)(src + q);
+        dst[q] = make_float2(v.x, v.z);
+    }
+}
+
+static int convert(Plan &P, const void *src, void *dst, bool to_ff, const char *what) {
+    const size_t n = P.field_elems();
+    {
+        Launch L_(P, what, 32.0 * n);
+        if (to_ff) k_d2q<<<152 * 8, 256, 0, P.stream>>>((const double2 *)src, (ffc *)dst, n);
+        else k_q2d<<<152 * 8, 256, 0, P.stream>>>((const ffc *)src, (double2 *)dst, n);
+    }
+    return check_launch(what);
 }
 
 // The harmonic correction of sol_project forward-transforms a(z) = c1 p1 + c2 p2 and
@@ -135,7 +177,17 @@ int fused_create(Plan &P, const StageParams &sp, FusedState **out) {
         cudaStreamDestroy(fs->nlp->stream);
         fs->nlp->stream = P.stream;
         fs->nlp->owner = &P;
-        for (int i = 0; i < fs->nc; i++) ok = ok && cudaMalloc(&fs->v32[i], fs->nlp->field_bytes()) == cudaSuccess;
+        for (int i = 0; i < fs->nc; i++) {
+            ok = ok && cudaMalloc(&fs->v32[i], fs->nlp->field_bytes()) == cudaSuccess;
+            ok = ok && cudaMalloc(&fs->vq[i], P.field_bytes()) == cudaSuccess;
+            ok = ok && cudaMalloc(&fs->cq[i], P.field_bytes()) == cudaSuccess;
+        }
+        ok = ok && cudaMalloc(&fs->prq, P.field_bytes()) == cudaSuccess;
+        if (ok && build_fft_table(fs->tzq, P.nz, FF)) {
+            fused_destroy(fs);
+            set_error("float-float FFT table construction failed");
+            return ERR_CUDA;
+        }
     }
     if (!ok) {
         cudaGetLastError();
@@ -143,7 +195,10 @@ int fused_create(Plan &P, const StageParams &sp, FusedState **out) {
         set_error("out of device memory (fused stage buffers)");
         return ERR_OOM;
     }
-    const int st = harmonic_spectra(P, fs->E[0], fs->E[1]);
+    int st = harmonic_spectra(P, fs->E[0], fs->E[1]);
+    // the float-float column kernels read the unit-profile spectra in float-float
+    for (int i = 0; i < 2 && !st && fs->nlp; i++) st = convert(P, fs->E[i], fs->E[i], true, "spectra_to_ff");
+    if (!st && cudaStreamSynchronize(P.stream) != cudaSuccess) st = check_launch("fused stage setup");
     if (st) {
         fused_destroy(fs);
         return st;
@@ -161,7 +216,11 @@ unsigned long long fused_bytes(const Plan &P, const FusedState *fs) {
     for (int i = 0; i < 3; i++) b += fs->W[i] ? P.field_bytes() : 0;
     if (fs->nlp) {
         b += plan_bytes(*fs->nlp);
-        for (int i = 0; i < 4; i++) b += fs->v32[i] ? fs->nlp->field_bytes() : 0;
+        for (int i = 0; i < 4; i++) {
+            b += fs->v32[i] ? fs->nlp->field_bytes() : 0;
+            b += (fs->vq[i] ? P.field_bytes() : 0) + (fs->cq[i] ? P.field_bytes() : 0);
+        }
+        b += fs->prq ? P.field_bytes() : 0;
     }
     return b;
 }
@@ -177,17 +236,26 @@ void fused_destroy(FusedState *fs) {
         if (fs->E[i]) cudaFree(fs->E[i]);
     for (int i = 0; i < 3; i++)
         if (fs->W[i]) cudaFree(fs->W[i]);
-    for (int i = 0; i < 4; i++)
+    for (int i = 0; i < 4; i++) {
         if (fs->v32[i]) cudaFree(fs->v32[i]);
+        if (fs->vq[i]) cudaFree(fs->vq[i]);
+        if (fs->cq[i]) cudaFree(fs->cq[i]);
+    }
+    if (fs->prq) cudaFree(fs->prq);
+    free_fft_table(fs->tzq);
     if (fs->nlp) plan_destroy(fs->nlp);
     delete fs;
 }
 
 template <typename T>
-static int launch(Plan &P, const FusedArgs &a, int which, double bytes) {
-    const int st = fast_fused(P, a, which, bytes);
-    if (st != kNoFast) return st;
-    return launch_fused<T, GenericFFT<T>>(P, P.tz.d, a, which, bytes);
+static int launch(Plan &P, const FusedState *fs, const FusedArgs &a, int which, double bytes) {
+    if constexpr (is_ff<T>) {
+        return launch_fused<ff, GenericFFT<ff>>(P, fs->tzq.d, a, which, bytes);
+    } else {
+        const int st = fast_fused(P, a, which, bytes);
+        if (st != kNoFast) return st;
+        return launch_fused<T, GenericFFT<T>>(P, P.tz.d, a, which, bytes);
+    }
 }
 
 template <typename T>
@@ -204,7 +272,8 @@ static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], c
         const size_t n = P.field_elems();
         for (int i = 0; i < fs->nc; i++) {
             Launch L_(P, "narrow_state", 24.0 * n);
-            k_narrow<<<152 * 8, 256, 0, P.stream>>>((const double2 *)vin[i], (float2 *)fs->v32[i], n);
+            if constexpr (is_ff<T>) k_q2f<<<152 * 8, 256, 0, P.stream>>>((const ffc *)vin[i], (float2 *)fs->v32[i], n);
+            else k_narrow<<<152 * 8, 256, 0, P.stream>>>((const double2 *)vin[i], (float2 *)fs->v32[i], n);
         }
         if ((st = check_launch("narrow_state"))) return st;
         const void *v3[3] = {fs->v32[0], fs->v32[1], fs->v32[2]};
@@ -215,9 +284,12 @@ static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], c
             if (!(spec[c] = Q.scratch_field(16 + c))) { set_error("out of device memory (NL spectra)"); return ERR_OOM; }
         st = Ops<float>::nonlinear(Q, v3, bouss ? fs->v32[3] : nullptr, spec, 0, bouss ? 4 : 3, nullptr);
         for (int c = 0; c < 4; c++) nl[c] = spec[c];
-    } else {
+    } else if constexpr (!is_ff<T>) {
         const void *v3[3] = {vin[0], vin[1], vin[2]};
         st = Ops<T>::nonlinear(P, v3, bouss ? vin[3] : nullptr, nullptr, 0, bouss ? 4 : 3, nl);
+    } else {
+        set_error("float-float stages need the FP32 companion plan");
+        return ERR_STATE;
     }
     if (st) return st;
     FusedArgs a{};
@@ -255,15 +327,15 @@ static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], c
         // and the unit-profile spectra in, vout and pr rows out
         const double bc = row * (3.0 * nlr + (6.0 + (bouss ? 1 : 0)) * P.nz + 3.0 * P.nz);
         const double bp = row * ((3.0 + 2.0) * P.nz + 3.0 * P.nz + P.nzp);
-        if ((st = launch<T>(P, a, kFusedVComp, bc))) return st;
-        if ((st = launch<T>(P, a, kFusedVProj, bp))) return st;
-    } else if ((st = launch<T>(P, a, kFusedVelocity, bv))) {
+        if ((st = launch<T>(P, fs, a, kFusedVComp, bc))) return st;
+        if ((st = launch<T>(P, fs, a, kFusedVProj, bp))) return st;
+    } else if ((st = launch<T>(P, fs, a, kFusedVelocity, bv))) {
         return st;
     }
     if (bouss) {
         const double bt = row * (1.0 * nlr + 3.0 * P.nz + 1.0 * P.nz);
-        if ((st = launch<T>(P, a, kFusedTheta, bt))) return st;
-        if (!rot && (st = launch<T>(P, a, kFusedHerm, 4.0 * P.ny * P.nz * P.elt()))) return st;
+        if ((st = launch<T>(P, fs, a, kFusedTheta, bt))) return st;
+        if (!rot && (st = launch<T>(P, fs, a, kFusedHerm, 4.0 * P.ny * P.nz * P.elt()))) return st;
     }
     return OK;
 }
@@ -285,14 +357,41 @@ static int step_impl(Plan &P, FusedState *fs, void *const v[4], void *pr) {
     return check_launch("fused step");
 }
 
-int fused_step(Plan &P, FusedState *fs, void *const v[4], void *pr) {
-    return P.prec == FP64 ? step_impl<double>(P, fs, v, pr) : step_impl<float>(P, fs, v, pr);
+int fused_step(Plan &P, FusedState *fs, void *const v[4], void *pr, int nsteps) {
+    if (fs->nlp) {
+        // nl_fp32: the state in float-float for the whole call
+        int st = OK;
+        for (int i = 0; i < fs->nc && !st; i++) st = convert(P, v[i], fs->vq[i], true, "state_to_ff");
+        if (!st) st = convert(P, pr, fs->prq, true, "state_to_ff");
+        for (int t = 0; t < nsteps && !st; t++) st = step_impl<ff>(P, fs, fs->vq, fs->prq);
+        for (int i = 0; i < fs->nc && !st; i++) st = convert(P, fs->vq[i], v[i], false, "state_from_ff");
+        if (!st) st = convert(P, fs->prq, pr, false, "state_from_ff");
+        return st;
+    }
+    for (int t = 0; t < nsteps; t++) {
+        const int st = P.prec == FP64 ? step_impl<double>(P, fs, v, pr) : step_impl<float>(P, fs, v, pr);
+        if (st) return st;
+    }
+    return OK;
 }
 
 int fused_stage(Plan &P, FusedState *fs, int o, void *const v[4], void *pr, const void *const Cold[4]) {
     const void *vin[4] = {v[0], v[1], v[2], v[3]};
-    int st = P.prec == FP64 ? run_stage<double>(P, fs, o, vin, Cold, fs->X1, pr)
-                            : run_stage<float>(P, fs, o, vin, Cold, fs->X1, pr);
+    int st;
+    if (fs->nlp) {
+        st = OK;
+        for (int i = 0; i < fs->nc && !st; i++) st = convert(P, v[i], fs->vq[i], true, "state_to_ff");
+        for (int i = 0; i < fs->nc && !st; i++) st = convert(P, Cold[i], fs->cq[i], true, "state_to_ff");
+        if (!st) st = convert(P, pr, fs->prq, true, "state_to_ff");
+        const void *vq[4] = {fs->vq[0], fs->vq[1], fs->vq[2], fs->vq[3]};
+        const void *cq[4] = {fs->cq[0], fs->cq[1], fs->cq[2], fs->cq[3]};
+        if (!st) st = run_stage<ff>(P, fs, o, vq, cq, fs->X1, fs->prq);
+        for (int i = 0; i < fs->nc && !st; i++) st = convert(P, fs->X1[i], v[i], false, "state_from_ff");
+        if (!st) st = convert(P, fs->prq, pr, false, "state_from_ff");
+        return st;
+    }
+    st = P.prec == FP64 ? run_stage<double>(P, fs, o, vin, Cold, fs->X1, pr)
+                        : run_stage<float>(P, fs, o, vin, Cold, fs->X1, pr);
     if (st) return st;
     for (int i = 0; i < fs->nc; i++) cudaMemcpyAsync(v[i], fs->X1[i], P.field_bytes(), cudaMemcpyDeviceToDevice, P.stream);
     return check_launch("fused stage");

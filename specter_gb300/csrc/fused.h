@@ -15,7 +15,7 @@ void fused_destroy(FusedState *fs);
 int fused_stage(Plan &P, FusedState *fs, int o, void *const v[4], void *pr, const void *const Cold[4]);
 // one full RK step on the state v: stages ord..1 with the step start held in v itself
 // (stage outputs ping-pong through the state's own buffers; no copies)
-int fused_step(Plan &P, FusedState *fs, void *const v[4], void *pr);
+int fused_step(Plan &P, FusedState *fs, void *const v[4], void *pr, int nsteps = 1);
 // device bytes held by the fused-stage buffers (0 for a null state)
 unsigned long long fused_bytes(const Plan &P, const FusedState *fs);
 

@@ -42,11 +42,15 @@ struct FusedArgs {
     int nl_spec;          // (with nl32) the NL fields are already z spectra: rows [0, nz), the
                           // forward transform with continuation done by the FP32 pipeline
     float f_dt, f_nu, f_kappa, f_rmp, f_xmom, f_xtemp, f_wall_tmp, f_omega[3];  // FP32 mirrors
+    ff q_dt, q_nu, q_kappa, q_rmp, q_xmom, q_xtemp, q_wall_tmp, q_omega[3];      // float-float
     FusedArgs prepared() const {
         FusedArgs b = *this;
         b.f_dt = (float)dt; b.f_nu = (float)nu; b.f_kappa = (float)kappa; b.f_rmp = (float)rmp;
         b.f_xmom = (float)xmom; b.f_xtemp = (float)xtemp; b.f_wall_tmp = (float)wall_tmp;
         for (int i = 0; i < 3; i++) b.f_omega[i] = (float)omega[i];
+        b.q_dt = ff(dt); b.q_nu = ff(nu); b.q_kappa = ff(kappa); b.q_rmp = ff(rmp);
+        b.q_xmom = ff(xmom); b.q_xtemp = ff(xtemp); b.q_wall_tmp = ff(wall_tmp);
+        for (int i = 0; i < 3; i++) b.q_omega[i] = ff(omega[i]);
         return b;
     }
 };
@@ -63,6 +67,9 @@ struct LapCol {
 template <typename T> __device__ __forceinline__ T exp_t(T x);
 template <> __device__ __forceinline__ float exp_t<float>(float x) { return expf(x); }
 template <> __device__ __forceinline__ double exp_t<double>(double x) { return exp(x); }
+// float-float kernels use exp only for the bulk rows of the pressure potential, an output that
+// no later stage reads (its wall rows are set exactly); FP32 accuracy there
+template <> __device__ __forceinline__ ff exp_t<ff>(ff x) { return ff(expf(x.hi)); }
 
 // The same profile on the bulk rows, in the kernel's precision (they enter the z transform
 // in that precision).
@@ -95,6 +102,84 @@ __device__ __forceinline__ void lap_coef_neumann(const Geo &g, int kx, int ky, d
 template <typename T>
 __device__ __forceinline__ double2 d2(C2<T> v) { return make_double2((double)v.x, (double)v.y); }
 
+// Wall values of a column as running sums over its spectrum: s0 = sum_k v_k (bottom wall) and
+// s1 = sum_k v_k w_k (top wall, w = Geo::wtw).  FP64 sums for the FP32 and FP64 kernels (four
+// FP64 fused multiply-adds per point: the FP64 pipe bounds that loop), float-float sums for the
+// float-float kernels.  Partials are reduced over a warp by shuffles and stored as two 16-byte
+// slots per (warp, column).
+template <typename T>
+struct WallSum {
+    static constexpr bool kFF = is_ff<T>;
+    double2 d0, d1;
+    ffc q0, q1;
+    __device__ __forceinline__ WallSum() {
+        d0 = d1 = make_double2(0.0, 0.0);
+        q0.x = q0.y = q1.x = q1.y = ff(0);
+    }
+    __device__ __forceinline__ void add(const Geo &g, C2<T> v, int k) {
+        if constexpr (kFF) {
+            const ffc w = ldg_v((const ffc *)g.wtwq + k);
+            q0.x += v.x;
+            q0.y += v.y;
+            q1.x += v.x * w.x - v.y * w.y;
+            q1.y += v.x * w.y + v.y * w.x;
+        } else {
+            const double vr = (double)v.x, vi = (double)v.y;
+            const double2 w = ((const double2 *)g.wtw)[k];
+            d0.x += vr;
+            d0.y += vi;
+            d1.x = fma(vr, w.x, d1.x);
+            d1.x = fma(-vi, w.y, d1.x);
+            d1.y = fma(vr, w.y, d1.y);
+            d1.y = fma(vi, w.x, d1.y);
+        }
+    }
+    __device__ __forceinline__ static ff shfl(ff v, int off) {
+        return ff(__shfl_xor_sync(0xffffffffu, v.hi, off), __shfl_xor_sync(0xffffffffu, v.lo, off));
+    }
+    // sum over the lanes c, c + TK, ... of a warp
+    __device__ __forceinline__ void warp_reduce(int TK) {
+        for (int off = TK; off < 32; off <<= 1) {
+            if constexpr (kFF) {
+                q0.x += shfl(q0.x, off);
+                q0.y += shfl(q0.y, off);
+                q1.x += shfl(q1.x, off);
+                q1.y += shfl(q1.y, off);
+            } else {
+                d0.x += __shfl_xor_sync(0xffffffffu, d0.x, off);
+                d0.y += __shfl_xor_sync(0xffffffffu, d0.y, off);
+                d1.x += __shfl_xor_sync(0xffffffffu, d1.x, off);
+                d1.y += __shfl_xor_sync(0xffffffffu, d1.y, off);
+            }
+        }
+    }
+    __device__ __forceinline__ void store(double2 *slot) const {
+        if constexpr (kFF) {
+            ((ffc *)slot)[0] = q0;
+            ((ffc *)slot)[1] = q1;
+        } else {
+            slot[0] = d0;
+            slot[1] = d1;
+        }
+    }
+    __device__ __forceinline__ void load_add(const double2 *slot) {
+        if constexpr (kFF) {
+            const ffc a = ((const ffc *)slot)[0], b = ((const ffc *)slot)[1];
+            q0.x += a.x; q0.y += a.y; q1.x += b.x; q1.y += b.y;
+        } else {
+            d0.x += slot[0].x; d0.y += slot[0].y; d1.x += slot[1].x; d1.y += slot[1].y;
+        }
+    }
+    __device__ __forceinline__ double2 bottom() const {
+        if constexpr (kFF) return make_double2(ff_to_double(q0.x), ff_to_double(q0.y));
+        else return d0;
+    }
+    __device__ __forceinline__ double2 top() const {
+        if constexpr (kFF) return make_double2(ff_to_double(q1.x), ff_to_double(q1.y));
+        else return d1;
+    }
+};
+
 // Tile of NL_c (rows [0, rows), columns col0 + [0, TK)): by asynchronous copies when the NL field
 // has the kernel's precision, else (FP32 NL fields in an FP64 kernel, the nl_fp32 form) by
 // converting loads, complete for the calling thread on return.  Either way one copy group is
@@ -102,18 +187,15 @@ __device__ __forceinline__ double2 d2(C2<T> v) { return make_double2((double)v.x
 template <typename T>
 __device__ __forceinline__ void nl_tile_load(C2<T> *dst, const FusedArgs &a, int c, unsigned col0, unsigned zs, int rows,
                                              int TK, int nv) {
-    if constexpr (sizeof(T) == 8) {
+    if constexpr (!is_f32<T>) {
         if (a.nl32) {
             const float2 *src = (const float2 *)a.nl[c] + col0;
             const int lgTK = lg2(TK);
             for (int idx = threadIdx.x; idx < rows * TK; idx += blockDim.x) {
                 const int k = idx >> lgTK, cc = idx & (TK - 1);
-                double2 v = make_double2(0.0, 0.0);
-                if (cc < nv) {
-                    const float2 f = __ldg(src + ((unsigned)k * zs + (unsigned)cc));
-                    v = make_double2((double)f.x, (double)f.y);
-                }
-                dst[idx] = v;
+                float2 f = make_float2(0.f, 0.f);
+                if (cc < nv) f = __ldg(src + ((unsigned)k * zs + (unsigned)cc));
+                dst[idx] = from_f2<T>(f);
             }
             async_commit();
             return;
@@ -132,7 +214,7 @@ template <typename T, class E>
 __device__ __forceinline__ C2<T> *nl_forward(const Geo &g, const typename E::Desc &fd, const FusedArgs &a, C2<T> *X,
                                              C2<T> *Y, int TK) {
     __syncthreads();
-    if constexpr (sizeof(T) == 8) {
+    if constexpr (!is_f32<T>) {
         if (a.nl_spec) return X;
     }
     fc_continuation<T>(g, X, TK);
@@ -175,8 +257,8 @@ __device__ void vel_update(const Geo &g, const typename E::Desc &fd, const Fused
     const int nz = g.nz, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
     const int tile = nz * TK;
     const bool stage2 = (size_t)E::kBuffers * fd.L >= 2 * (size_t)nz;  // vin and cold both fit in X
-    const T dt = pick<T>(a.dt, a.f_dt), nu = pick<T>(a.nu, a.f_nu), rmp = pick<T>(a.rmp, a.f_rmp);
-    const T xmom = pick<T>(a.xmom, a.f_xmom);
+    const T dt = pick<T>(a.dt, a.f_dt, a.q_dt), nu = pick<T>(a.nu, a.f_nu, a.q_nu), rmp = pick<T>(a.rmp, a.f_rmp, a.q_rmp);
+    const T xmom = pick<T>(a.xmom, a.f_xmom, a.q_xmom);
     V *R = nl_forward<T, E>(g, fd, a, X, Y, TK);
     if (buoy) {
         async_wait();
@@ -184,8 +266,8 @@ __device__ void vel_update(const Geo &g, const typename E::Desc &fd, const Fused
     }
     // (a) filtered nonlinear term (+ 2 Om x v, minus buoyancy) -> Uc
     const V *va = (const V *)a.vin[(c3 + 1) % 3], *vb = (const V *)a.vin[(c3 + 2) % 3];
-    const T oa = pick<T>(a.omega[(c3 + 1) % 3], a.f_omega[(c3 + 1) % 3]);
-    const T ob = pick<T>(a.omega[(c3 + 2) % 3], a.f_omega[(c3 + 2) % 3]);
+    const T oa = pick<T>(a.omega[(c3 + 1) % 3], a.f_omega[(c3 + 1) % 3], a.q_omega[(c3 + 1) % 3]);
+    const T ob = pick<T>(a.omega[(c3 + 2) % 3], a.f_omega[(c3 + 2) % 3], a.q_omega[(c3 + 2) % 3]);
     for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
         const int k = idx >> lgTK, c = idx & (TK - 1);
         V n = mk<T>(0, 0);
@@ -238,7 +320,7 @@ __device__ void vel_walls(const Geo &g, const typename E::Desc &fd, const FusedA
     using V = C2<T>;
     const int nz = g.nz, nzp = g.nzp, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
     const V *pr = (const V *)a.pr;
-    const T wall_tmp = pick<T>(a.wall_tmp, a.f_wall_tmp), inz = (T)1 / (T)nz;
+    const T wall_tmp = pick<T>(a.wall_tmp, a.f_wall_tmp, a.q_wall_tmp), inz = (T)1 / (T)nz;
     if (!in_x) {
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) X[idx] = Uc[idx];
         __syncthreads();
@@ -290,14 +372,13 @@ __device__ void vel_project(const Geo &g, const typename E::Desc &fd, const Fuse
     const int nz = g.nz, nzp = g.nzp, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
     const int tile = nz * TK;
     const bool stage2 = (size_t)E::kBuffers * fd.L >= 2 * (size_t)nz;
-    const double2 *wtw = (const double2 *)g.wtw;
     LapCol<T> *lcol = (LapCol<T> *)(coef + 2 * TK);
     // ---- Poisson: d -> X (natural), v -= i k d, wall sums of vz (FP64)
     {
         const int c = threadIdx.x & (TK - 1), k0 = threadIdx.x >> lgTK, kstep = blockDim.x >> lgTK;
         const int kxc = min(kx0 + c, g.nxh - 1);
         const T kx_ = g.KX<T>(kxc), ky_ = g.KY<T>(ky);
-        double2 s0 = make_double2(0, 0), s1 = make_double2(0, 0);
+        WallSum<T> ws;
         if (threadIdx.x < kstep * TK) {
             for (int k = k0; k < nz; k += kstep) {
                 const int idx = k * TK + c;
@@ -306,7 +387,7 @@ __device__ void vel_project(const Geo &g, const typename E::Desc &fd, const Fuse
                 V A = U[idx], B = U[tile + idx], Cc = U[2 * tile + idx];
                 const V s = mk<T>(kx_ * A.x + ky_ * B.x + kz_ * Cc.x, kx_ * A.y + ky_ * B.y + kz_ * Cc.y);
                 V D;
-                if constexpr (sizeof(T) == 4) {  // FP32-bulk: one division per point
+                if constexpr (!is_f64<T>) {  // FP32 and float-float: one reciprocal per point
                     const T ik2 = (T)1 / k2;
                     D = mk<T>(s.y * ik2, -s.x * ik2);
                 } else {
@@ -318,39 +399,21 @@ __device__ void vel_project(const Geo &g, const typename E::Desc &fd, const Fuse
                 Cc = csub(Cc, cimk(kz_, D));
                 U[idx] = A; U[tile + idx] = B; U[2 * tile + idx] = Cc;
                 X[idx] = D;
-                const double vr = (double)Cc.x, vi = (double)Cc.y;
-                const double2 w = wtw[k];
-                s0.x += vr; s0.y += vi;
-                // the top wall: s1 += v w as four FP64 fused multiply-adds (the FP64 pipe, two
-                // operations per clock per SM, bounds this loop)
-                s1.x = fma(vr, w.x, s1.x);
-                s1.x = fma(-vi, w.y, s1.x);
-                s1.y = fma(vr, w.y, s1.y);
-                s1.y = fma(vi, w.x, s1.y);
+                ws.add(g, Cc, k);
             }
         }
         // sum over the threads of a column: shuffles within each warp (the lanes of column c are
         // c, c + TK, ...), then one partial per warp
-        for (int off = TK; off < 32; off <<= 1) {
-            s0.x += __shfl_xor_sync(0xffffffffu, s0.x, off);
-            s0.y += __shfl_xor_sync(0xffffffffu, s0.y, off);
-            s1.x += __shfl_xor_sync(0xffffffffu, s1.x, off);
-            s1.y += __shfl_xor_sync(0xffffffffu, s1.y, off);
-        }
+        ws.warp_reduce(TK);
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        if (lane < TK) {
-            red[2 * (warp * TK + lane)] = s0;
-            red[2 * (warp * TK + lane) + 1] = s1;
-        }
+        if (lane < TK) ws.store(red + 2 * (warp * TK + lane));
     }
     __syncthreads();
     if (threadIdx.x < TK) {
         const int c = threadIdx.x, nwarps = blockDim.x >> 5;
-        double2 b1 = make_double2(0, 0), b2 = make_double2(0, 0);
-        for (int q = 0; q < nwarps; q++) {
-            const double2 p0 = red[2 * (q * TK + c)], p1 = red[2 * (q * TK + c) + 1];
-            b1.x += p0.x; b1.y += p0.y; b2.x += p1.x; b2.y += p1.y;
-        }
+        WallSum<T> tot;
+        for (int q = 0; q < nwarps; q++) tot.load_add(red + 2 * (q * TK + c));
+        double2 b1 = tot.bottom(), b2 = tot.top();
         const double inz = 1.0 / nz;  // wall values of vz / nz
         b1.x *= inz; b1.y *= inz; b2.x *= inz; b2.y *= inz;
         const int kxc = min(kx0 + c, g.nxh - 1);
@@ -376,6 +439,16 @@ __device__ void vel_project(const Geo &g, const typename E::Desc &fd, const Fuse
             if (c >= nv) continue;
             V pa, pb;
             lap_profile_t<T>(lcol[c], g.ZZ<T>(k), Lz, pa, pb);
+            if constexpr (is_ff<T>) {
+                // the wall rows feed the next stage's no-slip planes: exact profile values there
+                // (p1 = exp(-kh Lz), p2 = 1 at z = 0; p1 = 1, p2 = exp(-kh Lz) at z = Lz)
+                const LapCol<T> &p = lcol[c];
+                if ((k == 0 || k == nzp - 1) && !p.k0) {
+                    const ff e(g.lapc[((size_t)ky * g.nxh + min(kx0 + c, g.nxh - 1)) * 3 + 1]);
+                    pa = k == 0 ? mk<T>(p.c1.x * e + p.c2.x, p.c1.y * e + p.c2.y)
+                                : mk<T>(p.c1.x + p.c2.x * e, p.c1.y + p.c2.y * e);
+                }
+            }
             const V dv = R[E::pos(k, fd) * TK + c];
             prw[fidx<T>(g, k, ky, kx0 + c)] = mk<T>(dv.x * inz + pa.x, dv.y * inz + pa.y);
         }
@@ -495,7 +568,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_vcomp(Geo g, 
 
 // Split form, part 2: the projection of the three components written by k_fused_vcomp.
 template <typename T, class E, int CTK = 0>
-__global__ void __launch_bounds__(kThreads, 2) k_fused_vproj(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
+__global__ void __launch_bounds__(kThreads, is_ff<T> ? 1 : 2) k_fused_vproj(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
     const int TK = CTK ? CTK : TKrt;  // CTK: the tile width fixed at compile time, else 0
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -529,8 +602,8 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
     const int kx0 = blockIdx.x * TK, ky = blockIdx.y;
     const int nv = min(TK, g.nxh - kx0);
     auto colq = [&](int z, int c) { return fidx<T>(g, z, ky, kx0 + c); };
-    const T dt = pick<T>(a.dt, a.f_dt), kap = pick<T>(a.kappa, a.f_kappa), rmp = pick<T>(a.rmp, a.f_rmp);
-    const T inz = (T)1 / (T)nz, xtemp = pick<T>(a.xtemp, a.f_xtemp);
+    const T dt = pick<T>(a.dt, a.f_dt, a.q_dt), kap = pick<T>(a.kappa, a.f_kappa, a.q_kappa), rmp = pick<T>(a.rmp, a.f_rmp, a.q_rmp);
+    const T inz = (T)1 / (T)nz, xtemp = pick<T>(a.xtemp, a.f_xtemp, a.q_xtemp);
     // 1. NL_theta forward, heat current, filter, laplak, update.  vz is copied into Th while
     //    NL_theta is transformed; theta and cold go into the FFT buffer afterwards.
     {
@@ -670,7 +743,8 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_theta_herm(Geo g, t
         const int k = idx >> lgTK, c = idx & (TK - 1);
         const V p = s1[k], m = s2[k];
         // column c = 0 holds ky, c = 1 holds -ky
-        const V h = c == 0 ? mk<T>((T)0.5 * (p.x + m.x), (T)0.5 * (p.y - m.y)) : mk<T>((T)0.5 * (m.x + p.x), (T)0.5 * (m.y - p.y));
+        const T half = T(0.5f);
+        const V h = c == 0 ? mk<T>(half * (p.x + m.x), half * (p.y - m.y)) : mk<T>(half * (m.x + p.x), half * (m.y - p.y));
         X[idx] = h;
     }
     __syncthreads();

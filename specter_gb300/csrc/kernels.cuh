@@ -35,8 +35,15 @@ __device__ __forceinline__ unsigned fidx(const Geo &g, int z, int ky, int kx) {
 // register cap gets rematerialised per element on the FP64 pipe (1/64 rate here).
 template <typename T>
 __device__ __forceinline__ T pick(double d, float f) {
-    if constexpr (sizeof(T) == 8) return d;
+    if constexpr (is_f64<T>) return d;
     else return f;
+}
+// the same with a float-float mirror, for kernels that also run in float-float
+template <typename T>
+__device__ __forceinline__ T pick(double d, float f, ff q) {
+    if constexpr (is_f64<T>) return d;
+    else if constexpr (is_f32<T>) return f;
+    else return q;
 }
 
 template <typename T>
@@ -195,26 +202,46 @@ __device__ __forceinline__ void fc_continuation(const Geo &g, C2<T> *X, int TK) 
     __shared__ double2 wv[2 * kMaxOz * kMaxTile];
     const int lgTK = lg2(TK);
     const int C = g.cz, d = g.oz, n = g.nz;
-    for (int idx = threadIdx.x; idx < 2 * d * TK; idx += blockDim.x) {
-        const int j = idx >> lgTK, c = idx & (TK - 1);
-        const int row = j < d ? n - C - d + j : d - 1 - (j - d);
-        const C2<T> v = X[row * TK + c];
-        wv[idx] = make_double2((double)v.x, (double)v.y);
-    }
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < C * TK; idx += blockDim.x) {
-        const int ii = idx >> lgTK, c = idx & (TK - 1);
-        const double2 t0 = wv[c], b0 = wv[d * TK + c];
-        const double a0 = __ldg(g.dir + ii), a1 = __ldg(g.dir + (C - 1 - ii));
-        double ar = a0 * t0.x + a1 * b0.x;
-        double ai = a0 * t0.y + a1 * b0.y;
-        for (int jj = 1; jj < d; jj++) {
-            const double2 t = wv[jj * TK + c], b = wv[(d + jj) * TK + c];
-            const double w0 = __ldg(g.dir + ii + C * jj), w1 = __ldg(g.dir + (C - 1 - ii) + C * jj);
-            ar = ar + w0 * t.x + w1 * b.x;
-            ai = ai + w0 * t.y + w1 * b.y;
+    if constexpr (is_ff<T>) {
+        // float-float kernels: the sums in float-float with dir split into float-float pairs
+        for (int idx = threadIdx.x; idx < C * TK; idx += blockDim.x) {
+            const int ii = idx >> lgTK, c = idx & (TK - 1);
+            ff ar(0), ai(0);
+            for (int jj = 0; jj < d; jj++) {
+                const C2<T> t = X[(n - C - d + jj) * TK + c], b = X[(d - 1 - jj) * TK + c];
+                const float2 q0 = __ldg((const float2 *)(g.dirq + ii + C * jj));
+                const float2 q1 = __ldg((const float2 *)(g.dirq + (C - 1 - ii) + C * jj));
+                const ff w0(q0.x, q0.y), w1(q1.x, q1.y);
+                ar = ar + w0 * t.x + w1 * b.x;
+                ai = ai + w0 * t.y + w1 * b.y;
+            }
+            C2<T> r;
+            r.x = ar;
+            r.y = ai;
+            X[(n - C + ii) * TK + c] = r;
         }
-        X[(n - C + ii) * TK + c] = mk<T>((T)ar, (T)ai);
+    } else {
+        for (int idx = threadIdx.x; idx < 2 * d * TK; idx += blockDim.x) {
+            const int j = idx >> lgTK, c = idx & (TK - 1);
+            const int row = j < d ? n - C - d + j : d - 1 - (j - d);
+            const C2<T> v = X[row * TK + c];
+            wv[idx] = make_double2((double)v.x, (double)v.y);
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < C * TK; idx += blockDim.x) {
+            const int ii = idx >> lgTK, c = idx & (TK - 1);
+            const double2 t0 = wv[c], b0 = wv[d * TK + c];
+            const double a0 = __ldg(g.dir + ii), a1 = __ldg(g.dir + (C - 1 - ii));
+            double ar = a0 * t0.x + a1 * b0.x;
+            double ai = a0 * t0.y + a1 * b0.y;
+            for (int jj = 1; jj < d; jj++) {
+                const double2 t = wv[jj * TK + c], b = wv[(d + jj) * TK + c];
+                const double w0 = __ldg(g.dir + ii + C * jj), w1 = __ldg(g.dir + (C - 1 - ii) + C * jj);
+                ar = ar + w0 * t.x + w1 * b.x;
+                ai = ai + w0 * t.y + w1 * b.y;
+            }
+            X[(n - C + ii) * TK + c] = mk<T>((T)ar, (T)ai);
+        }
     }
 }
 
@@ -272,7 +299,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass_t(Geo g, typ
     const V *in = (const V *)a.in[f];
     const int nv = min(TK, g.nxh - kx0);
     const T sc = pick<T>(a.scale, a.scale_f);
-    const bool scaled = sizeof(T) == 8 ? a.scale != 1.0 : a.scale_f != 1.0f;
+    const bool scaled = is_f64<T> ? a.scale != 1.0 : a.scale_f != 1.0f;
     const V *src = in + (unsigned)z * g.ny * g.ldx + kx0;
     if (a.staged) tile_load_async(S, src, (unsigned)g.ldx, g.ny, TK, nv);
     for (int pass = 1; pass >= 0; pass--) {  // derivative output first: out0 may alias in
@@ -423,7 +450,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_r2c(Geo g, typena
     __syncthreads();
     if (a.scale != 1.0) {
         const T sc = pick<T>(a.scale, a.scale_f);
-    const bool scaled = sizeof(T) == 8 ? a.scale != 1.0 : a.scale_f != 1.0f;
+    const bool scaled = is_f64<T> ? a.scale != 1.0 : a.scale_f != 1.0f;
         for (int idx = threadIdx.x; idx < g.nxh * SP; idx += blockDim.x) S[idx] = cscale(S[idx], sc);
     }
     __syncthreads();
@@ -451,7 +478,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_c2r(Geo g, typena
     V *R = E::run(X, Y, RB, fd, +1);
     const int H = g.H;
     const T sc = pick<T>(a.scale, a.scale_f);
-    const bool scaled = sizeof(T) == 8 ? a.scale != 1.0 : a.scale_f != 1.0f;
+    const bool scaled = is_f64<T> ? a.scale != 1.0 : a.scale_f != 1.0f;
     for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x) {
         const int m = idx >> lgRB, r = idx & (RB - 1);
         V v = R[E::pos(m, fd) * RB + r];

@@ -63,10 +63,17 @@ int build_fft_table(FFTTable &t, int n, Prec prec) {
     if (nf < 0) return ERR_SHAPE;
     d.L = L;
     d.nst = nf;
-    const size_t es = prec == FP64 ? 16 : 8;
+    const size_t es = prec == FP32 ? 8 : 16;
     const size_t ntot = (size_t)L + (d.blue ? (size_t)n + 2 * (size_t)L : 0);
     std::vector<char> h(ntot * es);
-    auto P = [&](size_t i, const cld &v) { if (prec == FP64) put<double>(h, i * es, v); else put<float>(h, i * es, v); };
+    auto P = [&](size_t i, const cld &v) {
+        if (prec == FP64) put<double>(h, i * es, v);
+        else if (prec == FP32) put<float>(h, i * es, v);
+        else {
+            const ff q[2] = {ff_split(v.real()), ff_split(v.imag())};
+            memcpy(h.data() + i * es, q, sizeof q);
+        }
+    };
     for (int k = 0; k < L; k++) P(k, root(k, L));
     if (d.blue) {
         const long double pi = 3.14159265358979323846264338327950288L;
@@ -252,6 +259,10 @@ int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], cons
         std::vector<float> gf(g.begin(), g.end());
         if (cudaMalloc(&p->dgeof, gf.size() * sizeof(float)) != cudaSuccess) { set_error("cudaMalloc failed"); plan_destroy(p); return ERR_OOM; }
         cudaMemcpy(p->dgeof, gf.data(), gf.size() * sizeof(float), cudaMemcpyHostToDevice);
+        std::vector<ff> gq(g.size());
+        for (size_t i = 0; i < g.size(); i++) gq[i] = ff_split(g[i]);
+        if (cudaMalloc(&p->dgeoq, gq.size() * sizeof(ff)) != cudaSuccess) { set_error("cudaMalloc failed"); plan_destroy(p); return ERR_OOM; }
+        cudaMemcpy(p->dgeoq, gq.data(), gq.size() * sizeof(ff), cudaMemcpyHostToDevice);
     }
     // R2C / C2R post-processing twiddles exp(-2*pi*i*k/nx), k = 0..H
     {
@@ -283,6 +294,8 @@ int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], cons
     G.dir = p->dgeo + odir; G.fx = p->dgeo + ofx; G.fy = p->dgeo + ofy; G.fz = p->dgeo + ofz;
     G.kxf = p->dgeof + okx; G.kyf = p->dgeof + oky; G.kzf = p->dgeof + okz; G.zf = p->dgeof + oz_;
     G.fxf = p->dgeof + ofx; G.fyf = p->dgeof + ofy; G.fzf = p->dgeof + ofz;
+    G.kxq = p->dgeoq + okx; G.kyq = p->dgeoq + oky; G.kzq = p->dgeoq + okz; G.zq = p->dgeoq + oz_;
+    G.fxq = p->dgeoq + ofx; G.fyq = p->dgeoq + ofy; G.fzq = p->dgeoq + ofz; G.dirq = p->dgeoq + odir;
     G.xtw = p->dxtw;
     {
         // laplace_z constants of every (kx, ky) column (boundary_mod.fpp:521-549)
@@ -313,6 +326,15 @@ int plan_create(Plan **out, const int n[3], const int c[3], const int o[3], cons
         cudaMalloc(&p->dwtw, w.size() * sizeof(double));
         cudaMemcpy(p->dwtw, w.data(), w.size() * sizeof(double), cudaMemcpyHostToDevice);
         G.wtw = p->dwtw;
+        std::vector<ff> wq(2 * (size_t)nz);  // (re, im) pairs of float-float: an ffc per k
+        for (int k = 0; k < nz; k++) {
+            cld v = std::conj(root((long)k * (p->nzp - 1), nz));
+            wq[2 * k] = ff_split(v.real());
+            wq[2 * k + 1] = ff_split(v.imag());
+        }
+        cudaMalloc(&p->dwtwq, wq.size() * sizeof(ff));
+        cudaMemcpy(p->dwtwq, wq.data(), wq.size() * sizeof(ff), cudaMemcpyHostToDevice);
+        G.wtwq = p->dwtwq;
     }
     cudaMallocHost(&p->hred, sizeof(double) * 64);
     if (cudaGetLastError() != cudaSuccess) { set_error("CUDA error during plan creation"); plan_destroy(p); return ERR_CUDA; }
@@ -399,6 +421,8 @@ void plan_destroy(Plan *p) {
     free_fft4_table(p->tx4); free_fft4_table(p->ty4); free_fft4_table(p->tz4);
     if (p->dgeo) cudaFree(p->dgeo);
     if (p->dgeof) cudaFree(p->dgeof);
+    if (p->dgeoq) cudaFree(p->dgeoq);
+    if (p->dwtwq) cudaFree(p->dwtwq);
     if (p->dlapc) cudaFree(p->dlapc);
     if (p->dxtw) cudaFree(p->dxtw);
     if (p->dred) cudaFree(p->dred);

@@ -10,7 +10,9 @@
 
 namespace sg {
 
-enum Prec { FP64 = 0, FP32 = 1 };
+// Plans are FP64 or FP32; FF (float-float) is the precision of internal tables and kernels of
+// the precision form on FP64 plans.
+enum Prec { FP64 = 0, FP32 = 1, FF = 2 };
 
 // error status shared with the C-ABI (include/specter_gpu.h)
 enum Status {
@@ -44,21 +46,26 @@ struct Geo {
     const double *fx, *fy, *fz;               // fc_filter factors per axis (FP64)
     const float *kxf, *kyf, *kzf, *zf;         // the same tables rounded to FP32, so FP32
     const float *fxf, *fyf, *fzf;             // kernels do no FP64 conversion per element
+    const ff *kxq, *kyq, *kzq, *zq;           // and split into float-float pairs, for the
+    const ff *fxq, *fyq, *fzq, *dirq;         // float-float kernels of the precision form
     const double *lapc;                       // per (ky, kx) column: kh, exp(-kh Lz), Neumann 1/(kh (1 - exp(-2 kh Lz)))
     const void *xtw;                          // C2<T>[H+1]: exp(-2*pi*i*k/nx)
     const void *wtw;                          // double2[nz]: exp(+2*pi*i*k*(nzp-1)/nz)
+    const void *wtwq;                         // the same as float-float complex (ffc[nz])
     double Lz;
     // table entries in the kernel's precision: (T)kx[i], read from the matching table
-#define SG_GEO_TABLE(NAME, D, F) \
+#define SG_GEO_TABLE(NAME, D, F, Q) \
     template <typename T> __device__ __forceinline__ T NAME(int i) const { \
-        if constexpr (sizeof(T) == 8) return __ldg(D + i); else return __ldg(F + i); }
-    SG_GEO_TABLE(KX, kx, kxf)
-    SG_GEO_TABLE(KY, ky, kyf)
-    SG_GEO_TABLE(KZ, kz, kzf)
-    SG_GEO_TABLE(ZZ, z, zf)
-    SG_GEO_TABLE(FX, fx, fxf)
-    SG_GEO_TABLE(FY, fy, fyf)
-    SG_GEO_TABLE(FZ, fz, fzf)
+        if constexpr (is_f64<T>) return __ldg(D + i); \
+        else if constexpr (is_f32<T>) return __ldg(F + i); \
+        else { const float2 v = __ldg((const float2 *)(Q + i)); return ff(v.x, v.y); } }
+    SG_GEO_TABLE(KX, kx, kxf, kxq)
+    SG_GEO_TABLE(KY, ky, kyf, kyq)
+    SG_GEO_TABLE(KZ, kz, kzf, kzq)
+    SG_GEO_TABLE(ZZ, z, zf, zq)
+    SG_GEO_TABLE(FX, fx, fxf, fxq)
+    SG_GEO_TABLE(FY, fy, fyf, fyq)
+    SG_GEO_TABLE(FZ, fz, fzf, fzq)
 #undef SG_GEO_TABLE
 };
 
@@ -73,6 +80,8 @@ struct Plan {
     std::vector<double> kx, ky, kz, z, dir, fx, fy, fz;
     double *dgeo = nullptr;   // device block holding kx, ky, kz, z, dir, fx, fy, fz
     float *dgeof = nullptr;   // the same block rounded to FP32
+    ff *dgeoq = nullptr;      // and split into float-float pairs
+    void *dwtwq = nullptr;    // inverse-z twiddles at the top wall as float-float complex
     double *dlapc = nullptr;  // laplace_z column constants (Geo::lapc)
     void *dxtw = nullptr;
     FFTTable tx, ty, tz;      // lengths H = nx/2, ny, nz
