@@ -106,6 +106,32 @@ __device__ __forceinline__ ff &operator-=(ff &a, ff b) { a = ff_sub(a, b); retur
 __device__ __forceinline__ ff &operator*=(ff &a, ff b) { a = ff_mul(a, b); return a; }
 __device__ __forceinline__ ff &operator*=(ff &a, float b) { a = ff_mulf(a, b); return a; }
 
+// a b + c d with one renormalisation: exact leading products (FMA), TwoSum of them, every
+// lower-order term folded into the error word.  Normwise error ~u^2 (|a b| + |c d|): what a
+// complex multiply in an FFT needs.
+__device__ __forceinline__ ff ff_dot2(ff a, ff b, ff c, ff d) {
+    const float p1 = a.hi * b.hi, p2 = c.hi * d.hi;
+    const float e1 = fmaf(a.hi, b.hi, -p1), e2 = fmaf(c.hi, d.hi, -p2);
+    float s, t;
+    two_sum(p1, p2, s, t);
+    t += e1 + e2;
+    t = fmaf(a.hi, b.lo, t);
+    t = fmaf(a.lo, b.hi, t);
+    t = fmaf(c.hi, d.lo, t);
+    t = fmaf(c.lo, d.hi, t);
+    float h, l;
+    fast_two_sum(s, t, h, l);
+    return ff(h, l);
+}
+
+// complex float-float product: 38 flops (four exact products, two TwoSums)
+__device__ __forceinline__ ffc cmul(ffc a, ffc b) {
+    ffc r;
+    r.x = ff_dot2(a.x, b.x, ff_neg(a.y), b.y);
+    r.y = ff_dot2(a.x, b.y, a.y, b.x);
+    return r;
+}
+
 // conversions with FP64 (FP64 pipe: use at kernel boundaries only)
 __device__ __forceinline__ ff ff_from_double(double d) {
     const float h = __double2float_rn(d);

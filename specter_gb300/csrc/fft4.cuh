@@ -41,15 +41,18 @@ constexpr int pick_radix(int m) {
 // per translation unit: w_N^t = exp(-2 pi i t / N) for every N in kRegSizes
 static __constant__ float2 c_regtw_f[kRegTableLen];
 static __constant__ double2 c_regtw_d[kRegTableLen];
+static __constant__ ffc c_regtw_q[kRegTableLen];  // float-float
 
 template <typename T> __device__ __forceinline__ C2<T> regtw(int i);
 template <> __device__ __forceinline__ float2 regtw<float>(int i) { return c_regtw_f[i]; }
 template <> __device__ __forceinline__ double2 regtw<double>(int i) { return c_regtw_d[i]; }
+template <> __device__ __forceinline__ ffc regtw<ff>(int i) { return c_regtw_q[i]; }
 
 // upload the constant tables of this translation unit (host)
 static inline cudaError_t fft4_init_tables() {
     static float2 hf[kRegTableLen];
     static double2 hd[kRegTableLen];
+    static ffc hq[kRegTableLen];
     const long double pi = 3.14159265358979323846264338327950288L;
     for (int i = 0; i < kNumRegSizes; i++) {
         const int N = kRegSizes[i], off = reg_offset(N);
@@ -57,10 +60,13 @@ static inline cudaError_t fft4_init_tables() {
             long double a = -2.0L * pi * t / N;
             hd[off + t] = make_double2((double)cosl(a), (double)sinl(a));
             hf[off + t] = make_float2((float)cosl(a), (float)sinl(a));
+            hq[off + t].x = ff_split(cosl(a));
+            hq[off + t].y = ff_split(sinl(a));
         }
     }
     cudaError_t e = cudaMemcpyToSymbol(c_regtw_f, hf, sizeof hf);
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_regtw_d, hd, sizeof hd);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_regtw_q, hq, sizeof hq);
     return e;
 }
 

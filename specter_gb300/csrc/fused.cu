@@ -250,6 +250,10 @@ void fused_destroy(FusedState *fs) {
 template <typename T>
 static int launch(Plan &P, const FusedState *fs, const FusedArgs &a, int which, double bytes) {
     if constexpr (is_ff<T>) {
+        // the generic Stockham engine: in float-float its radix-8/5/3 butterflies with their
+        // trivial rotations done as swaps take fewer float-float multiplies than register DFTs
+        // of 8, 9 and 15 points with table twiddles (three passes instead of five: measured
+        // 30 % slower at 512^2 x 513)
         return launch_fused<ff, GenericFFT<ff>>(P, fs->tzq.d, a, which, bytes);
     } else {
         const int st = fast_fused(P, a, which, bytes);

@@ -7,7 +7,10 @@ grids of the ensemble and the served stream: z 90 = 10*9 directly, Bluestein 128
 FP32 rounding of the d wall-adjacent points is amplified by the continuation (sum |dir| = 9.5e3):
 rounding a smooth column to FP32 alone (2.5e-8) already gives ~2e-5 relative error in its
 continued spectrum (tests/test_fc_conditioning.py), so transforms through the continuation are
-held to 3e-4 and a stage to 1e-3 against the FP64 oracle; C2R (no continuation) to 1e-6."""
+held to 3e-4 against the FP64 oracle and C2R (no continuation) to 1e-6; one RK2 step to about 3x
+the largest error measured on these grids (fused velocity 1e-4, theta 1.5e-3).  This form does
+not meet 1e-5 after 1000 steps (its errors grow with the step count); the precision form that
+does is tests/test_gpu_precision.py."""
 import numpy as np
 import pytest
 
@@ -127,7 +130,12 @@ def test_stage_fp32(pair32, solver):
         outs[fused] = [f.download() for f in (s.vx, s.vy, s.vz)] + ([s.th.download()] if solver == 1 else [])
         errs = [rel(a, b) for a, b in zip(outs[fused], ref[: len(outs[fused])])]
         print("stage fused=%s" % fused, ["%.2e" % e for e in errs])
-        assert max(errs) < 1e-3
+        # about 3x the largest error measured over the six grids: fused velocity 3.3e-5, reference
+        # sequence velocity 3.0e-4 (its z component goes through two more FP32 continuations),
+        # theta (both paths) 4.2e-4
+        assert max(errs[:3]) < (1e-4 if fused else 1e-3)
+        if solver == 1:
+            assert errs[3] < 1.5e-3
     cons = [rel(a, b) for a, b in zip(outs[True], outs[False])]
     print("fused vs reference sequence", ["%.2e" % e for e in cons])
     assert max(cons) < 1e-3
@@ -173,4 +181,4 @@ def test_x_pass_eight_rows(shape):
     s.step(1)
     errs = [rel(f.download(), r) for f, r in zip((s.vx, s.vy, s.vz, s.th), ref[:4])]
     print("stage", ["%.2e" % e for e in errs])
-    assert max(errs) < 1e-3
+    assert max(errs[:3]) < 1e-4 and errs[3] < 1e-3  # measured: velocity <= 2.4e-5, theta 2.8e-4

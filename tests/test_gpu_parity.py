@@ -18,6 +18,7 @@ GRIDS = [
     (48, 12, 29, 1.0),   # nx/2 = 24, ny = 12 (radix 3), NZ = 54
     (32, 20, 129, 1.0),  # ny = 20 (radix 5), NZ = 154 = 2*7*11
     (64, 64, 65, 2.0),   # the plain-FP64 channel grid, NZ = 90
+    (32, 32, 513, 1.0),  # the Rayleigh-Benard z grid, NZ = 538 = 2*269 (Bluestein 1080)
 ]
 
 
@@ -236,3 +237,25 @@ def test_plan_limits():
     with pytest.raises(SpecterError) as e:
         api.Plan((16, 16, 64), (0, 0, 25), (0, 0, 10), (1.0, 1.0, 1.0), precision=1)
     assert e.value.code == 1
+
+
+def test_bouss_step_128x128x513():
+    """One FP64 RK2 step of the Rayleigh-Benard case on a 128 x 128 x 513 (+25) grid against the
+    oracle: fused stage kernels and the reference call sequence (bouss_rkstep2.f90:1-59)."""
+    from specter_gb300 import api, initial
+    plan, g = make_pair(128, 128, 513, 1.0)
+    th = g.fftp3d_real_to_complex(initial.convection_theta(plan, seed=20261203, amp=1e-3))
+    rng = np.random.default_rng(9)
+    v = [smooth_spectral(g, rng, amp=1e-3) for _ in range(3)]
+    pr = np.zeros(g.sshape, complex)
+    kw = dict(dt=1e-5, nu=1e-4, kappa=1e-4, ord=2)
+    ref = g.run(g.params(**kw), 1, *v, pr, th=th)
+    for fused in (True, False):
+        s = api.Solver(plan, api.BOUSS, fused=fused, **kw)
+        for f, a in zip((s.vx, s.vy, s.vz, s.th, s.pr), v + [th, pr]):
+            f.upload(a)
+        s.step(1)
+        got = [f.download() for f in (s.vx, s.vy, s.vz, s.th)]
+        for a, b in zip(got, ref[:4]):
+            assert rel(a, b) < 1e-11, fused
+        s.close()
