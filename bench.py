@@ -3,18 +3,24 @@
 Workload (one "step" = one RK2 step = 2 RK stages over the whole grid): the Boussinesq
 Rayleigh-Benard case, nx = ny = 512 (periodic, Lx = Ly = 2*pi), nz = 513 physical points
 (+ Cz = 25 FC-Gram continuation points, NZ = 538) on z in [0, 1], d = 5, Pr = 1,
-nu = kappa = 1e-4, RK order 2, dt = 1e-5, in the FP32-bulk precision form; seeded synthetic
-initial field (theta' = 1e-3 * U(-1,1) * z(1 - z), v = 0).  Each field is 566 MB, far larger
-than the 129 MB L2, so no L2 flush is needed between steps.
+nu = kappa = 1e-4, RK order 2, dt = 1e-5; seeded synthetic initial field
+(theta' = 1e-3 * U(-1,1) * z(1 - z), v = 0).  Each field is 566 MB (FP32) or 1.13 GB (FP64
+words), far larger than the 129 MB L2, so no L2 flush is needed between steps.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--form nl32|fp32|fp64] [--impl reference]
+
+The headline form (--form nl32, the default) is the precision form that keeps within 1e-5
+relative L2 of plain FP64 after 1000 steps: the nonlinear term in FP32, the state and every
+operation that carries it through a z transform in float-float (FP32 pairs).  Beside it the line
+reports plain FP64 (`fp64`), FP32-bulk (`fp32_bulk`, faster, but outside the 1e-5 gate) and
+`precision`: each form against plain FP64 after 10 steps in this run, with the committed
+1000-step record of profiles/precision_bouss512.md.
 
 Prints one JSON line (rank 0).  `value` is grid points x RK stages per second with the state
 resident in HBM; `e2e` is the same metric through the C ABI with the state uploaded from
-pinned host memory and downloaded back every step (median of the individually timed steps;
-the mean is printed beside it).  `--impl reference` times the FP64 CPU
-restatement of the reference algorithm (the oracle; the Fortran reference cannot be built
-here) on a bounded sample of the same workload on the host cores.
+pinned host memory and downloaded back every step (steps / total time).  `--impl reference`
+times the FP64 CPU restatement of the reference algorithm (the oracle; the Fortran reference
+cannot be built here) on a bounded sample of the same workload on the host cores.
 """
 from __future__ import annotations
 
@@ -156,11 +162,13 @@ def fp64_gemm_tflops(device):
     return 2.0 * 8192 ** 3 / best / 1e12
 
 
-def load_traffic():
+def load_traffic(form="fp32"):
     """Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of each kernel from
-    the committed ncu summary of this workload: the rows '| kernel | launches | bytes per launch |'
-    of profiles/dram_traffic_bouss512.md."""
-    path = os.path.join(ROOT, "profiles", "dram_traffic_bouss512.md")
+    the committed ncu summary of this workload and form: the rows
+    '| kernel | launches | bytes per launch |' of profiles/dram_traffic_bouss512.md (FP32-bulk)
+    or profiles/dram_traffic_bouss512_nl32.md (the precision form)."""
+    name = "dram_traffic_bouss512.md" if form == "fp32" else f"dram_traffic_bouss512_{form}.md"
+    path = os.path.join(ROOT, "profiles", name)
     out = {}
     try:
         for ln in open(path):
@@ -238,6 +246,60 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def time_steps(plan, s, K, local):
+    """K RK steps (one solver call) bracketed by CUDA events on the plan stream; returns ms."""
+    import torch
+    stream = torch.cuda.ExternalStream(plan.stream, device=torch.device("cuda", local))
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    s.step(K)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1)
+
+
+def physical_errors(api, p64, a, b, names):
+    """Relative L2 of each state field of solver a against solver b on the physical grid (FP64
+    c2r of both states, rows z < nzp)."""
+    import numpy as np
+    fc, fr = p64.field(api.COMPLEX), p64.field(api.REAL)
+
+    def phys(data):
+        fc.upload(np.ascontiguousarray(data, dtype=np.complex128))
+        api.fftp3d_complex_to_real(p64, fc, fr)
+        return fr.download()[: p64.nzp]
+    out = {}
+    for name, fa, fb in zip(names, (a.vx, a.vy, a.vz, a.th), (b.vx, b.vy, b.vz, b.th)):
+        ra, rb = phys(fa.download()), phys(fb.download())
+        nb = float(np.linalg.norm(rb))
+        out[name] = float(np.linalg.norm(ra - rb) / nb) if nb > 0 else float(np.linalg.norm(ra))
+    fc.close()
+    fr.close()
+    return out
+
+
+def committed_precision():
+    """The committed 1000-step record of the precision study (profiles/precision_bouss512.md,
+    its line starting with 'RESULT ')."""
+    path = os.path.join(ROOT, "profiles", "precision_bouss512.md")
+    try:
+        for ln in open(path):
+            if ln.startswith("RESULT "):
+                return json.loads(ln[len("RESULT "):])
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+FORMS = {
+    "nl32": "precision form: FP32 nonlinear term, float-float (FP32-pair) state and column kernels",
+    "fp32": "FP32-bulk (FP32 transforms and products; FP64 continuation arithmetic, wall solve, reductions)",
+    "fp64": "plain FP64",
+}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -249,13 +311,14 @@ def main():
     ap.add_argument("--grid", default=None, help="NX,NY,NZP: another grid of the same case (profiling, sweeps)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile widths")
     ap.add_argument("--caps", default=None, help="Z,Y,X,FUSED,SPLIT: set these instead of autotuning")
-    ap.add_argument("--fp64", action="store_true",
-                    help="the plain FP64 form instead of FP32-bulk (not the headline: reported against the FP64 peak)")
-    ap.add_argument("--form", default=None, choices=["fp32", "nl32", "fp64"],
-                    help="fp32: FP32-bulk plan; nl32: FP64 state with the nonlinear term in FP32; fp64: plain FP64")
+    ap.add_argument("--form", default="nl32", choices=sorted(FORMS),
+                    help="the timed form: nl32 (the precision form, default), fp32 (FP32-bulk), fp64 (plain)")
+    ap.add_argument("--fp64", action="store_true", help="same as --form fp64")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="time the chosen form only (no FP64 / FP32-bulk lines, no in-run precision check)")
     args = ap.parse_args()
-    if args.form == "fp64":
-        args.fp64 = True
+    if args.fp64:
+        args.form = "fp64"
     if args.impl == "reference":
         return run_reference(args)
 
@@ -275,11 +338,11 @@ def main():
     cfg = dict(CFG)
     if args.grid:
         cfg["nx"], cfg["ny"], cfg["nzp"] = (int(v) for v in args.grid.split(","))
-    nl32 = args.form == "nl32"
-    plan, s = build_solver(api, initial, cfg, api.FP64 if (args.fp64 or nl32) else api.FP32, fused=not args.refseq,
-                           nl_fp32=nl32)
+    form = args.form
+    prec = api.FP32 if form == "fp32" else api.FP64
+    plan, s = build_solver(api, initial, cfg, prec, fused=not args.refseq, nl_fp32=form == "nl32")
     # tile widths of each kernel family picked by timing RK steps (state restored afterwards)
-    if args.fp64:
+    if form == "fp64":
         caps = None
     elif args.caps:
         caps = [int(v) for v in args.caps.split(",")]
@@ -287,7 +350,6 @@ def main():
         api.set_option(plan, "velocity_split", caps[4])
     else:
         caps = s.autotune() if not args.no_autotune else None
-    stream = torch.cuda.ExternalStream(plan.stream, device=torch.device("cuda", local))
     for _ in range(W):
         s.step(1)
     plan.synchronize()
@@ -295,16 +357,8 @@ def main():
         dist.barrier()
     plan.profile(True)
     n0 = plan.launch_count
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        for _ in range(K):
-            s.step(1)
-        ev1.record(stream)
-        ev1.synchronize()
-        torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1)
+        ms = time_steps(plan, s, K, local)
     launches = plan.launch_count - n0
     report = plan.profile_report()
     plan.profile(False)
@@ -313,15 +367,14 @@ def main():
     pts = cfg["nx"] * cfg["ny"] * cfg["nzp"]
     value = job_throughput(world, pts, cfg["ord"] * K, ms * 1e-3)
 
-    # end to end: state uploaded from pinned host memory and downloaded every step
+    # end to end through the C ABI: the state uploaded from pinned host memory (reference layout)
+    # and downloaded back every step; value = steps / total time (the mean step)
     fields = [f for f in (s.vx, s.vy, s.vz, s.th, s.pr)]
     host = [torch.empty(f.nbytes, dtype=torch.uint8, pin_memory=True) for f in fields]
     ptrs = [h.data_ptr() for h in host]
     # one untimed round trip creates the staging buffers and the copy stream
     api.fields_download(fields, ptrs)
     api.fields_upload(fields, ptrs)
-    # each step timed on its own (host clock, data back on the host at the end of each); the
-    # median step is reported: the machine's host-link copies now and then take 20-50 % longer
     Ke = max(5, K // 2)
     plan.synchronize()
     if dist:
@@ -334,33 +387,30 @@ def main():
         api.fields_download(fields, ptrs)   # device -> pinned host, returns with the data on the host
         plan.synchronize()
         tsteps.append(time.perf_counter() - t0)
-    te = max_over_ranks(statistics.median(tsteps), dist, f"cuda:{local}")
+    te = max_over_ranks(sum(tsteps) / len(tsteps), dist, f"cuda:{local}")
     e2e = job_throughput(world, pts, cfg["ord"], te)
     nbytes = sum(f.nbytes for f in fields)
 
+    line = None
     if rank == 0:
-        field_mb = (cfg["nx"] // 2 + 1) * cfg["ny"] * (cfg["nzp"] + cfg["cz"]) * 8 / 1e6
+        field_mb = (cfg["nx"] // 2 + 1) * cfg["ny"] * (cfg["nzp"] + cfg["cz"]) * (16 if form != "fp32" else 8) / 1e6
         peak, peak_kind = peaks()
-        roof = dominant_roofline(report, peak, load_traffic())
+        roof = dominant_roofline(report, peak, load_traffic(form))
         roof["peak_kind"] = peak_kind
-        # stage-level model of the frozen measurement definition: B = 128 * N * s per BOUSS stage
+        # stage-level model of the frozen measurement definition: B = 128 * N * s per BOUSS stage,
+        # s the word size of the state (FP64-sized words for the FP64 and precision forms)
         N = cfg["nx"] * cfg["ny"] * (cfg["nzp"] + cfg["cz"])
-        es = 8 if args.fp64 else 4
+        es = 4 if form == "fp32" else 8
         model_gbs = 128 * N * es * cfg["ord"] * K / (ms * 1e-3) / 1e9
-        # secondary figure: model FFT flops per second against the FP32 CUDA-core FMA rate at the
-        # maximum SM clock (152 SMs x 128 lanes x 2), or against measured DGEMM for the FP64 form
-        flops = fft_flops_per_stage(cfg, plan.engines["z"]) * cfg["ord"] * K / (ms * 1e-3) / 1e12
-        if args.fp64:
-            fpeak, fkind = fp64_gemm_tflops(f"cuda:{local}"), "measured FP64 DGEMM (torch.matmul 8192^3)"
-        else:
-            fpeak, fkind = 152 * 128 * 2 * 2.07e9 / 1e12, "nominal FP32 FMA rate at 2070 MHz"
         line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": K,
                 "warmup": W, "ms_per_step": round(ms / K, 4), "higher_is_better": True,
-                "scaling": "weak" if world > 1 else "weak", "vs_baseline": None, "dtype": "f64" if args.fp64 else "f32",
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": {"nl32": "f32 (nonlinear) + f32x2 float-float (state, column kernels)", "fp32": "f32",
+                          "fp64": "f64"}[form],
                 "data": "synthetic",
                 "config": {"workload": f"BOUSS Rayleigh-Benard {cfg['nx']}x{cfg['ny']}x{cfg['nzp']} (+{cfg['cz']} FC-Gram, "
-                                       f"NZ={cfg['nzp'] + cfg['cz']}), {'plain FP64' if args.fp64 else 'FP32-bulk'}, "
-                                       f"RK2, dt=1e-5",
+                                       f"NZ={cfg['nzp'] + cfg['cz']}), RK2, dt=1e-5",
+                           "form": form, "form_detail": FORMS[form],
                            "path": "reference-sequence" if args.refseq else "fused",
                            "autotune_caps_z_y_x_fused_split": list(caps) if caps else None,
                            "l2": f"inputs larger than L2 ({field_mb:.0f} MB per field), no flush",
@@ -368,25 +418,93 @@ def main():
                 "roofline": roof,
                 "stage_model": {"bytes_per_stage": 128 * N * es, "achieved_gbs": round(model_gbs, 1),
                                 "frac": round(model_gbs / peak, 4)},
-                "fft_flops": {"per_stage": round(fft_flops_per_stage(cfg, plan.engines["z"])),
-                              "achieved_tflops": round(flops, 2), "peak_tflops": round(fpeak, 1),
-                              "peak_kind": fkind, "frac": round(flops / fpeak, 4)},
                 "kernels": {k: {"launches": v[0], "ms": round(v[1], 3),
                                 "gbs": round(v[2] / (v[1] * 1e-3) / 1e9, 1) if v[1] > 0 else None}
                             for k, v in sorted(report.items(), key=lambda kv: -kv[1][1])},
                 "clocks": clocks.summary(),
                 "e2e": {"value": round(e2e, 2), "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                        "steps": Ke, "median_ms_per_step": round(1e3 * statistics.median(tsteps), 3),
-                        "mean_ms_per_step": round(1e3 * statistics.mean(tsteps), 3),
+                        "steps": Ke, "mean_ms_per_step": round(1e3 * statistics.mean(tsteps), 3),
+                        "median_ms_per_step": round(1e3 * statistics.median(tsteps), 3),
                         "ms_per_step_each": [round(1e3 * t, 1) for t in tsteps]},
                 "gpu_launches": launches}
-        if not args.no_cpu and not args.fp64 and world == 1:
+        if not args.no_extra and world == 1 and not args.grid:
+            extra_forms(api, initial, cfg, local, form, line, peak, caps)
+        if not args.no_cpu and world == 1:
             v, cores, sample = cpu_baseline(1, 0)
             line["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def extra_forms(api, initial, cfg, local, form, line, peak, caps):
+    """The other forms of the same workload, beside the headline: plain FP64 (the reference's
+    own precision, with its roofline against HBM and against the measured FP64 peak) and
+    FP32-bulk; and the precision check: each form against plain FP64 after 10 steps from the
+    same initial field (in run), with the committed 1000-step record."""
+    names = ["vx", "vy", "vz", "th"]
+    pts = cfg["nx"] * cfg["ny"] * cfg["nzp"]
+    N = cfg["nx"] * cfg["ny"] * (cfg["nzp"] + cfg["cz"])
+    # plain FP64: 2 timed steps
+    p64, s64 = build_solver(api, initial, cfg, api.FP64, fused=True)
+    s64.step(1)
+    p64.profile(True)
+    ms64 = time_steps(p64, s64, 2, local)
+    rep64 = p64.profile_report()
+    p64.profile(False)
+    v64 = pts * cfg["ord"] * 2 / (ms64 * 1e-3) / 1e6
+    fpeak = fp64_gemm_tflops(f"cuda:{local}")
+    flops64 = fft_flops_per_stage(cfg, p64.engines["z"]) * cfg["ord"] * 2 / (ms64 * 1e-3) / 1e12
+    model64 = 128 * N * 8 * cfg["ord"] * 2 / (ms64 * 1e-3) / 1e9
+    line["fp64"] = {"value": round(v64, 2), "unit": UNIT, "ms_per_step": round(ms64 / 2, 3), "steps": 2,
+                    "roofline_hbm": {"stage_model_gbs": round(model64, 1), "peak": peak, "frac": round(model64 / peak, 4)},
+                    "roofline_fp64": {"model_fft_tflops": round(flops64, 3), "peak_tflops": round(fpeak, 3),
+                                      "peak_kind": "measured FP64 DGEMM (torch.matmul 8192^3)",
+                                      "frac": round(flops64 / fpeak, 4)},
+                    "kernels_ms_per_step": {k: round(v[1] / 2, 2)
+                                            for k, v in sorted(rep64.items(), key=lambda kv: -kv[1][1])[:6]}}
+    s64.close()
+    p64.close()
+    # FP32-bulk: autotuned, 10 timed steps
+    if form != "fp32":
+        p32, s32 = build_solver(api, initial, cfg, api.FP32, fused=True)
+        s32.autotune()
+        for _ in range(3):
+            s32.step(1)
+        p32.profile(True)
+        ms32 = time_steps(p32, s32, 10, local)
+        rep32 = p32.profile_report()
+        p32.profile(False)
+        roof32 = dominant_roofline(rep32, peak, load_traffic("fp32"))
+        line["fp32_bulk"] = {"value": round(pts * cfg["ord"] * 10 / (ms32 * 1e-3) / 1e6, 2), "unit": UNIT,
+                             "ms_per_step": round(ms32 / 10, 3), "roofline": roof32,
+                             "stage_model": {"bytes_per_stage": 128 * N * 4,
+                                             "frac": round(128 * N * 4 * cfg["ord"] * 10 / (ms32 * 1e-3) / 1e9 / peak, 4)}}
+        s32.close()
+        p32.close()
+    # precision: every form against plain FP64 after 10 steps from the same initial field
+    q64, r64 = build_solver(api, initial, cfg, api.FP64, fused=True)
+    r64.step(10)
+    prec = {"steps": 10, "reference": "plain FP64 GPU form (matches the FP64 oracle to 1e-11)",
+            "metric": "relative L2 on the physical grid"}
+    for f_ in ("nl32", "fp32"):
+        pf, sf = build_solver(api, initial, cfg, api.FP32 if f_ == "fp32" else api.FP64, fused=True,
+                              nl_fp32=f_ == "nl32")
+        if f_ == form and caps:
+            api.set_tile_caps(pf, caps[:4])
+            api.set_option(pf, "velocity_split", caps[4])
+        sf.step(10)
+        prec[f_] = physical_errors(api, q64, sf, r64, names)
+        sf.close()
+        pf.close()
+    r64.close()
+    q64.close()
+    rec = committed_precision()
+    line["precision"] = {"gate": "<= 1e-5 relative L2 against FP64 after 1000 steps", "in_run_10_steps": prec,
+                         "committed_1000_steps": rec,
+                         "meets_gate": {"nl32": bool(rec and rec.get("max_1000", 1.0) <= 1e-5),
+                                        "fp32": False}}
 
 
 if __name__ == "__main__":
