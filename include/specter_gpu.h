@@ -190,7 +190,9 @@ typedef struct specter_graph specter_graph;
 int specter_solver_autotune(specter_solver *s, int caps[5]);
 int specter_plan_tile_caps(specter_plan *plan, const int caps[4]);
 /* named plan options: "velocity_split" (0/1: fused velocity stage as one kernel or as a
- * per-component kernel plus a projection kernel), "tile_cap_z|y|x|fused" (1, 2, 4, 8, 16) */
+ * per-component kernel plus a projection kernel), "tile_cap_z|y|x|fused" (1, 2, 4, 8, 16),
+ * "ff_threads" (256 or 384: threads per block of the float-float column kernels of nl_fp32
+ * solvers; the autotuner picks it for those solvers) */
 int specter_plan_set_option(specter_plan *plan, const char *name, int value);
 int specter_graph_create(specter_solver *const *solvers, int n, int nsteps, specter_graph **out);
 int specter_graph_launch(specter_graph *g);

@@ -666,6 +666,11 @@ int specter_plan_set_option(specter_plan *plan, const char *name, int value) {
     if (!name) { set_error("null option name"); return SPECTER_ERR_ARG; }
     Plan &P = *plan->p;
     if (!strcmp(name, "velocity_split")) { P.velocity_split = value ? 1 : 0; return SPECTER_OK; }
+    if (!strcmp(name, "ff_threads")) {
+        if (value != 256 && value != 384) { set_error("ff_threads is 256 or 384"); return SPECTER_ERR_ARG; }
+        P.ff_threads = value;
+        return SPECTER_OK;
+    }
     const char *caps[4] = {"tile_cap_z", "tile_cap_y", "tile_cap_x", "tile_cap_fused"};
     for (int i = 0; i < 4; i++)
         if (!strcmp(name, caps[i])) {
@@ -717,6 +722,14 @@ int specter_solver_autotune(specter_solver *s, int caps[5]) {
         P.velocity_split = !keep;
         const float ms_other = trial();
         if (!(ms_other < ms_keep)) P.velocity_split = keep;
+        st = snap.put_back(s);
+    }
+    if (!st && s->fused && s->sp.nl_fp32) {  // block size of the float-float column kernels
+        const int keep = P.ff_threads;
+        const float ms_keep = trial();
+        P.ff_threads = keep == 384 ? 256 : 384;
+        const float ms_other = trial();
+        if (!(ms_other < ms_keep)) P.ff_threads = keep;
         st = snap.put_back(s);
     }
     cudaEventDestroy(e0);

@@ -254,7 +254,8 @@ static int launch(Plan &P, const FusedState *fs, const FusedArgs &a, int which, 
         // trivial rotations done as swaps take fewer float-float multiplies than register DFTs
         // of 8, 9 and 15 points with table twiddles (three passes instead of five: measured
         // 30 % slower at 512^2 x 513)
-        return launch_fused<ff, GenericFFT<ff>>(P, fs->tzq.d, a, which, bytes);
+        if (P.ff_threads == 256) return launch_fused<ff, GenericFFT<ff, 256>>(P, fs->tzq.d, a, which, bytes);
+        return launch_fused<ff, GenericFFT<ff, 384>>(P, fs->tzq.d, a, which, bytes);
     } else {
         const int st = fast_fused(P, a, which, bytes);
         if (st != kNoFast) return st;

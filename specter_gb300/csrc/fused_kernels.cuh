@@ -534,7 +534,7 @@ __global__ void __launch_bounds__(E::kWideThreads, 1) k_fused_velocity(Geo g, ty
 // vx and vy, the wall round trip; the result goes to W[c] (a stage buffer).  smem = Uc[nz][TK] +
 // FFT buffer(s): half the footprint of k_fused_velocity, so two blocks share an SM.
 template <typename T, class E, int CTK = 0>
-__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_vcomp(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
+__global__ void __launch_bounds__(E::kColThreads, E::kMinBlocks) k_fused_vcomp(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
     const int TK = CTK ? CTK : TKrt;  // CTK: the tile width fixed at compile time, else 0
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -568,7 +568,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_vcomp(Geo g, 
 
 // Split form, part 2: the projection of the three components written by k_fused_vcomp.
 template <typename T, class E, int CTK = 0>
-__global__ void __launch_bounds__(kThreads, is_ff<T> ? 1 : 2) k_fused_vproj(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
+__global__ void __launch_bounds__(E::kColThreads, is_ff<T> ? 1 : 2) k_fused_vproj(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
     const int TK = CTK ? CTK : TKrt;  // CTK: the tile width fixed at compile time, else 0
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -590,7 +590,7 @@ __global__ void __launch_bounds__(kThreads, is_ff<T> ? 1 : 2) k_fused_vproj(Geo 
 // scalar column kernel (Boussinesq): smem = Th[nz][TK] + E::kBuffers * L * TK
 // ----------------------------------------------------------------------------------------------
 template <typename T, class E, int CTK = 0>
-__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
+__global__ void __launch_bounds__(E::kColThreads, E::kMinBlocks) k_fused_theta(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
     const int TK = CTK ? CTK : TKrt;  // CTK: the tile width fixed at compile time, else 0
     const int lgTK = lg2(TK);
     using V = C2<T>;
@@ -727,7 +727,7 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_fused_theta(Geo g, 
 // kx = 0 and kx = nx/2 columns of the theta round trip: (X(ky) + conj X(-ky))/2, then continuation
 // and forward z transform.  One block per (kx column, ky pair); two columns per block.
 template <typename T, class E>
-__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_theta_herm(Geo g, typename E::Desc fd, FusedArgs a) {
+__global__ void __launch_bounds__(E::kColThreads, E::kMinBlocks) k_theta_herm(Geo g, typename E::Desc fd, FusedArgs a) {
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nzp = g.nzp, nz = g.nz, L = fd.L;

@@ -16,7 +16,7 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
     const size_t L = (size_t)fd.L;
     auto smem = [&](int tk) -> size_t {
         if (which == kFusedVelocity || which == kFusedVProj) {
-            const size_t thr = which == kFusedVelocity ? (size_t)E::wide_threads(tk) : (size_t)kThreads;
+            const size_t thr = which == kFusedVelocity ? (size_t)E::wide_threads(tk) : (size_t)E::kColThreads;
             return (3 * (size_t)P.nz + E::kBuffers * L) * tk * es + (2 * thr + (size_t)tk * 2) * 16 +
                    (size_t)tk * sizeof(LapCol<T>);
         }
@@ -29,7 +29,9 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
         // the one-kernel velocity stage needs all three components: one block per SM; the others
         // (including the projection, which holds the three components but transforms once) keep
         // two blocks per SM
-        const size_t budget = which == kFusedVelocity ? 200 * 1024 : 110 * 1024;
+        // (float-float kernels run one block per SM anyway, their registers allow no more: they
+        // may use most of the SM's shared memory)
+        const size_t budget = which == kFusedVelocity ? 200 * 1024 : is_ff<T> ? 220 * 1024 : 110 * 1024;
         for (int t : {16, 8, 4, 2, 1})
             if (t <= P.tile_cap[Plan::kTileFused] && smem(t) <= budget) { tk = t; break; }
         if (!tk) { set_error("z length too large for the fused column kernels"); return ERR_SHAPE; }
@@ -48,21 +50,21 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
     } else if (which == kFusedVComp) {
         auto k = (FIX && tk == FIX) ? k_fused_vcomp<T, E, FIX> : k_fused_vcomp<T, E>;
         if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k<<<dim3(cdiv(P.nxh, tk), P.ny, 3), kThreads, sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
+        k<<<dim3(cdiv(P.nxh, tk), P.ny, 3), E::kColThreads, sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
     } else if (which == kFusedVProj) {
         // the projection holds three components, so at the same cap it runs half the width of
         // the other column kernels: its own fixed-width copy at FIX / 2
         auto k = (FIX && tk == FIX) ? k_fused_vproj<T, E, FIX> : (FIX && tk == FIX / 2) ? k_fused_vproj<T, E, FIX / 2> : k_fused_vproj<T, E>;
         if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k<<<dim3(cdiv(P.nxh, tk), P.ny), kThreads, sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
+        k<<<dim3(cdiv(P.nxh, tk), P.ny), E::kColThreads, sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
     } else if (which == kFusedTheta) {
         auto k = (FIX && tk == FIX) ? k_fused_theta<T, E, FIX> : k_fused_theta<T, E>;
         if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k<<<dim3(cdiv(P.nxh, tk), P.ny), kThreads, sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
+        k<<<dim3(cdiv(P.nxh, tk), P.ny), E::kColThreads, sm, P.stream>>>(P.geo, fd, a.prepared(), tk);
     } else {
         auto k = k_theta_herm<T, E>;
         if (sm > 40 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        k<<<dim3(P.ny, 2), kThreads, sm, P.stream>>>(P.geo, fd, a.prepared());
+        k<<<dim3(P.ny, 2), E::kColThreads, sm, P.stream>>>(P.geo, fd, a.prepared());
     }
     P.prof_end();
     cudaError_t e = cudaGetLastError();

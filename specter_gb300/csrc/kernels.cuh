@@ -46,13 +46,18 @@ __device__ __forceinline__ T pick(double d, float f, ff q) {
     else return q;
 }
 
-template <typename T>
+// NT: threads per block of the column kernels that run this engine (kColThreads).  The
+// float-float column kernels take 255 registers a thread, so one block fills an SM's register
+// file at 256 threads; 384 threads at a 170-register cap give 12 warps instead of 8 to hide
+// the latency of the dependent float-float chains (plan option "ff_threads").
+template <typename T, int NT = kThreads>
 struct GenericFFT {
     using Desc = FFTDesc;
     static constexpr int kBuffers = 2;
     static constexpr int kMinBlocks = 1;
-    static constexpr int kWideThreads = kThreads;
-    static int wide_threads(int) { return kThreads; }
+    static constexpr int kColThreads = NT;
+    static constexpr int kWideThreads = NT;
+    static int wide_threads(int) { return NT; }
     static __device__ __forceinline__ C2<T> *run(C2<T> *X, C2<T> *Y, int B, const Desc &d, int sign) {
         return fft_exec<T>(X, Y, B, d, sign);
     }
@@ -71,6 +76,7 @@ struct FourStep {
     using Desc = FFT4Desc;
     static constexpr int kBuffers = 1;
     static constexpr int kMinBlocks = 2;  // cap registers at 128 so two blocks share an SM
+    static constexpr int kColThreads = kThreads;
     // Kernels that run one block per SM (the fused velocity kernel) may take enough threads for
     // one item per thread in both steps at a tile width of 8: 8 * max(L1, L2) rounded up to a
     // warp, at least kThreads.  With 36 x 30 that is 288, so the 288 items of step B do not leave
