@@ -204,6 +204,24 @@ int specter_graph_query(specter_graph *g, int *done);  /* 1 when every launch so
 int specter_solver_memory(specter_solver *s, unsigned long long *bytes);
 int specter_graph_destroy(specter_graph *g);
 
+/* ---- batched ensembles (no reference counterpart: the ensemble form).
+ * specter_batch_create records one RK step of each of n fused FP32 HD solvers (each on a plan
+ *      of its own; RK order >= 2; the split velocity stage is selected on their plans) and
+ *      captures it as one CUDA graph of batched launches: the i-th kernel of every solver's
+ *      step runs as one launch per distinct kernel (FFT length class, tile width) over the tiles
+ *      of all the solvers that use it, so an ensemble of uneven grids takes a few dozen
+ *      launches a step instead of a few per solver.  Each solver computes exactly what its own
+ *      steps would.
+ * specter_batch_step advances every solver's state by nsteps RK steps (after the work already
+ *      queued on the solvers' plan streams); specter_batch_synchronize waits for it.
+ *      specter_batch_kernels gives the launches per step.  Destroy a batch before its solvers. */
+typedef struct specter_batch specter_batch;
+int specter_batch_create(specter_solver *const *solvers, int n, specter_batch **out);
+int specter_batch_step(specter_batch *b, int nsteps);
+int specter_batch_synchronize(specter_batch *b);
+int specter_batch_kernels(specter_batch *b, long long *kernels);
+int specter_batch_destroy(specter_batch *b);
+
 /* ---- timers: out = {ffttime, tratime, comtime, conttime, tottime, stages} in seconds,
  *      accumulated from CUDA events (the reference's fftp_mod.fpp:32-37 accumulators) */
 int specter_timers(specter_plan *plan, double out[6]);

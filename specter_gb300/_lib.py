@@ -37,6 +37,8 @@ EXPORTS = [
     "specter_table_check", "specter_fields_upload", "specter_fields_download",
     "specter_timers", "specter_timers_reset",
     "specter_profile", "specter_profile_report", "specter_launch_count",
+    "specter_batch_create", "specter_batch_step", "specter_batch_synchronize", "specter_batch_kernels",
+    "specter_batch_destroy",
 ]
 
 

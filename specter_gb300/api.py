@@ -466,4 +466,39 @@ class Graph:
             pass
 
 
+class Batch:
+    """Batched ensemble (specter_batch_create): one RK step of several fused FP32 HD solvers,
+    each on its own plan, as a few dozen batched launches captured in one CUDA graph; the i-th
+    kernel of every solver's step runs as one launch per FFT length class."""
+
+    def __init__(self, solvers):
+        self.solvers = list(solvers)
+        L = load()
+        self._L = L
+        arr = (C.c_void_p * len(self.solvers))(*[s.h.value for s in self.solvers])
+        h = C.c_void_p()
+        check(L.specter_batch_create(arr, len(self.solvers), C.byref(h)))
+        self.h = h
+        n = C.c_longlong()
+        check(L.specter_batch_kernels(h, C.byref(n)))
+        self.kernels = n.value
+
+    def step(self, n=1):
+        check(self._L.specter_batch_step(self.h, int(n)))
+
+    def synchronize(self):
+        check(self._L.specter_batch_synchronize(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._L.specter_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 __all__ = [n for n in dir() if not n.startswith("_")] + ["SpecterError"]

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "../../include/specter_gpu.h"
+#include "batch.h"
 #include "fused.h"
 #include "handles.h"
 #include "ops.h"
@@ -914,6 +915,161 @@ int specter_profile_report(specter_plan *plan, char *buf, int buflen) {
 int specter_launch_count(specter_plan *plan, long long *count) {
     CHECK_PLAN(plan);
     *count = plan->p->launches;
+    return SPECTER_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ batched ensembles
+
+// One RK step of several solvers as a sequence of batched launches (batch.h), captured once as a
+// CUDA graph: position i of the sequence is the i-th kernel of every solver's step, launched once
+// per distinct kernel (template instance and shared memory) over all the solvers that use it.
+struct specter_batch {
+    cudaStream_t stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    void *recs = nullptr;  // every record, device
+    long long kernels = 0;
+    std::vector<specter_solver *> solvers;
+};
+
+extern "C" {
+
+int specter_batch_destroy(specter_batch *b) {
+    if (!b) return SPECTER_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->recs) cudaFree(b->recs);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return SPECTER_OK;
+}
+
+int specter_batch_create(specter_solver *const *solvers, int n, specter_batch **out) {
+    if (!solvers || n < 1 || !out) { set_error("bad batch arguments"); return SPECTER_ERR_ARG; }
+    *out = nullptr;
+    for (int i = 0; i < n; i++) {
+        specter_solver *s = solvers[i];
+        if (!s) { set_error("null solver"); return SPECTER_ERR_ARG; }
+        const Plan &P = *s->plan->p;
+        if (!s->fused || P.prec != FP32 || s->sp.solver != SPECTER_HD || s->sp.ord < 2 || s->sp.nl_fp32) {
+            set_error("batched ensembles take fused FP32 HD solvers of RK order >= 2");
+            return SPECTER_ERR_ARG;
+        }
+        if (P.profile) { set_error("batch with profiling enabled"); return SPECTER_ERR_STATE; }
+        for (int j = 0; j < i; j++)
+            if (solvers[j]->plan == s->plan) {  // their scratch fields would be shared within a launch
+                set_error("batched solvers need plans of their own");
+                return SPECTER_ERR_ARG;
+            }
+    }
+    // record one RK step of every solver (the split velocity form: its two kernels batch)
+    std::vector<Batch> rec(n);
+    int st = SPECTER_OK;
+    for (int i = 0; i < n && !st; i++) {
+        Plan &P = *solvers[i]->plan->p;
+        cudaStreamSynchronize(P.stream);
+        P.velocity_split = 1;
+        P.batch = &rec[i];
+        void *v[4] = {solvers[i]->v[0]->d, solvers[i]->v[1]->d, solvers[i]->v[2]->d, nullptr};
+        st = fused_step(P, solvers[i]->fs, v, solvers[i]->pr->d, 1);
+        P.batch = nullptr;
+        if (!st && rec[i].unbatchable) {
+            set_error(std::string("batch: launch without a batched form: ") + rec[i].unbatchable);
+            st = SPECTER_ERR_STATE;
+        }
+        if (!st && (rec[i].entries.size() != rec[0].entries.size())) {
+            set_error("batch: the solvers' steps have different kernel sequences");
+            st = SPECTER_ERR_STATE;
+        }
+        for (size_t k = 0; !st && k < rec[i].entries.size(); k++)
+            if (strcmp(rec[i].entries[k].name, rec[0].entries[k].name)) {
+                set_error("batch: the solvers' steps have different kernel sequences");
+                st = SPECTER_ERR_STATE;
+            }
+    }
+    if (st) return st;
+    // group each position by (kernel, shared memory); lay every group's records out contiguously
+    struct Group { const BatchEntry *proto; size_t off; int n, blocks; };
+    std::vector<Group> seq;
+    std::vector<unsigned char> host;
+    const size_t npos = rec[0].entries.size();
+    for (size_t k = 0; k < npos; k++) {
+        std::vector<int> used(n, 0);
+        for (int i = 0; i < n; i++) {
+            if (used[i]) continue;
+            const BatchEntry &e0 = rec[i].entries[k];
+            Group g{&e0, 0, 0, 0};
+            const size_t rsz = e0.rec.size();
+            host.resize((host.size() + 255) / 256 * 256);  // 256-byte aligned group start
+            g.off = host.size();
+            for (int j = i; j < n; j++) {
+                const BatchEntry &e = rec[j].entries[k];
+                if (used[j] || e.key != e0.key || e.smem != e0.smem || e.rec.size() != rsz) continue;
+                used[j] = 1;
+                const size_t at = host.size();
+                host.insert(host.end(), e.rec.begin(), e.rec.end());
+                BatchGrid *gr = (BatchGrid *)(host.data() + at);
+                gr->block0 = g.blocks;
+                g.blocks += e.blocks;
+                g.n++;
+            }
+            seq.push_back(g);
+        }
+    }
+    specter_batch *b = new specter_batch();
+    b->solvers.assign(solvers, solvers + n);
+    if (cudaMalloc(&b->recs, host.size()) != cudaSuccess) {
+        cudaGetLastError();
+        delete b;
+        set_error("out of device memory (batch records)");
+        return SPECTER_ERR_OOM;
+    }
+    cudaMemcpy(b->recs, host.data(), host.size(), cudaMemcpyHostToDevice);
+    cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+        st = check_launch("batch capture");
+        specter_batch_destroy(b);
+        return st ? st : SPECTER_ERR_CUDA;
+    }
+    for (const Group &g : seq) {
+        g.proto->launch((const unsigned char *)b->recs + g.off, g.n, g.blocks, g.proto->smem, b->stream);
+        b->kernels++;
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(b->stream, &graph);
+    b->graph = graph;
+    if (ec != cudaSuccess) { set_error(std::string("batch capture: ") + cudaGetErrorString(ec)); st = SPECTER_ERR_CUDA; }
+    if (!st && cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess) {
+        set_error("batch graph instantiation failed");
+        st = SPECTER_ERR_CUDA;
+    }
+    cudaGetLastError();
+    if (st) { specter_batch_destroy(b); return st; }
+    *out = b;
+    return SPECTER_OK;
+}
+
+int specter_batch_step(specter_batch *b, int nsteps) {
+    if (!b || nsteps < 0) { set_error("bad batch arguments"); return SPECTER_ERR_ARG; }
+    // work queued on the solvers' own streams (initial fields, earlier steps) comes first
+    for (specter_solver *s : b->solvers) cudaStreamSynchronize(s->plan->p->stream);
+    for (int t = 0; t < nsteps; t++)
+        if (cudaGraphLaunch(b->exec, b->stream) != cudaSuccess) return check_launch("batch launch");
+    return check_launch("batch launch");
+}
+
+int specter_batch_synchronize(specter_batch *b) {
+    if (!b) { set_error("null batch"); return SPECTER_ERR_ARG; }
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess) return check_launch("batch synchronize");
+    return SPECTER_OK;
+}
+
+int specter_batch_kernels(specter_batch *b, long long *kernels) {
+    if (!b || !kernels) { set_error("null argument"); return SPECTER_ERR_ARG; }
+    *kernels = b->kernels;
     return SPECTER_OK;
 }
 

@@ -54,6 +54,13 @@ int zinv(Plan &P, const ZInvArgs &a0, int nf, double bytes) {
     const size_t sm = per * tk;
     // the production z lengths (Bluestein 1080, 576) at tile width 8 run a copy with the width fixed
     constexpr bool kFixed = (L1 == 36 && L2 == 30) || (L1 == 24 && L2 == 24);
+    if (P.batch) {  // record for a batched launch (batch.h)
+        using R = PassRec<E, ZInvArgs>;
+        const R r{{0, cdiv(P.nxh, tk), P.ny, nf}, P.geo, P.tz4.d, a.prepared(), tk};
+        batch_add(*P.batch, r, (const void *)k_z_inverse_batch<float, E>, &batch_launch<R, k_z_inverse_batch<float, E>, kThreads>,
+                  sm, "z_inverse", bytes);
+        return OK;
+    }
     auto k = (kFixed && tk == 8) ? k_z_inverse<float, E, kFixed ? 8 : 0> : k_z_inverse<float, E>;
     smem_attr(k, sm);
     Scope s(P, "z_inverse", bytes);
@@ -82,6 +89,13 @@ int ypass(Plan &P, const YArgs &a0, int nf, int nplanes, double bytes) {
     const size_t sm = per * tk;
     // the production y lengths (512, 256) at tile width 16 run a copy with the width fixed
     constexpr bool kFixed = L2 == 16 && (L1 == 32 || L1 == 16);
+    if (P.batch) {  // record for a batched launch (batch.h)
+        using R = PassRec<E, YArgs>;
+        const R r{{0, cdiv(P.nxh, tk), nplanes, nf}, P.geo, P.ty4.d, a.prepared(), tk};
+        batch_add(*P.batch, r, (const void *)k_y_pass_batch<float, E>, &batch_launch<R, k_y_pass_batch<float, E>, kThreads>,
+                  sm, a.sign < 0 ? "y_forward" : "y_inverse", bytes);
+        return OK;
+    }
     auto k = (kFixed && tk == 16) ? k_y_pass_t<float, E, kFixed ? 16 : 0> : k_y_pass_t<float, E, 0>;
     smem_attr(k, sm);
     Scope s(P, a.sign < 0 ? "y_forward" : "y_inverse", bytes);
@@ -120,6 +134,13 @@ int xnl(Plan &P, const XNLArgs &a, double bytes) {
     const size_t sm = x_nl_elems<E>(P.tx4.d, P.nxh, P.H, rb) * sizeof(float2);
     // the production x lengths (H = 256, 128) at 8 rows run a copy with the row count fixed
     constexpr bool kFixed = L1 == 16 && (L2 == 16 || L2 == 8);
+    if (P.batch) {  // record for a batched launch (batch.h)
+        using R = PassRec<E, XNLArgs>;
+        const R r{{0, cdiv(a.nrows * P.ny, rb), 1, 1}, P.geo, P.tx4.d, a.prepared(), rb};
+        batch_add(*P.batch, r, (const void *)k_x_nonlinear_batch<float, E>,
+                  &batch_launch<R, k_x_nonlinear_batch<float, E>, kThreads>, sm, "x_nonlinear", bytes);
+        return OK;
+    }
     auto k = (kFixed && rb == 8) ? k_x_nonlinear<float, E, kFixed ? 8 : 0> : k_x_nonlinear<float, E>;
     smem_attr(k, sm);
     Scope s(P, "x_nonlinear", bytes);

@@ -231,13 +231,14 @@ struct ColTile {
     unsigned zs, col0;  // z stride of a column and the tile's first column offset
 };
 
+// bid: the block's index (blockIdx, or its instance-local index in a batched launch)
 template <typename T>
-__device__ __forceinline__ ColTile col_tile(const Geo &g, int TK) {
+__device__ __forceinline__ ColTile col_tile(const Geo &g, int TK, const uint3 &bid) {
     ColTile t;
     t.TK = TK;
     t.lgTK = lg2(TK);
-    t.kx0 = blockIdx.x * TK;
-    t.ky = blockIdx.y;
+    t.kx0 = bid.x * TK;
+    t.ky = bid.y;
     t.nv = min(TK, g.nxh - t.kx0);
     t.zs = (unsigned)g.ny * g.ldx;
     t.col0 = (unsigned)t.ky * g.ldx + t.kx0;
@@ -502,7 +503,7 @@ __global__ void __launch_bounds__(E::kWideThreads, 1) k_fused_velocity(Geo g, ty
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nz = g.nz, nzp = g.nzp, L = fd.L;
-    const ColTile t = col_tile<T>(g, TK);
+    const ColTile t = col_tile<T>(g, TK, blockIdx);
     const int tile = nz * TK;
     V *U = (V *)smem_raw;                       // 3 components, natural rows
     V *X = U + 3 * tile;                        // FFT work
@@ -533,13 +534,13 @@ __global__ void __launch_bounds__(E::kWideThreads, 1) k_fused_velocity(Geo g, ty
 // Split form, part 1: one block per (column tile, component): the component's update and, for
 // vx and vy, the wall round trip; the result goes to W[c] (a stage buffer).  smem = Uc[nz][TK] +
 // FFT buffer(s): half the footprint of k_fused_velocity, so two blocks share an SM.
-template <typename T, class E, int CTK = 0>
-__global__ void __launch_bounds__(E::kColThreads, E::kMinBlocks) k_fused_vcomp(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
+template <typename T, class E, int CTK>
+__device__ __forceinline__ void fused_vcomp_body(const Geo &g, const typename E::Desc &fd, const FusedArgs &a, int TKrt, uint3 blockIdx) {
     const int TK = CTK ? CTK : TKrt;  // CTK: the tile width fixed at compile time, else 0
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nz = g.nz, nzp = g.nzp;
-    const ColTile t = col_tile<T>(g, TK);
+    const ColTile t = col_tile<T>(g, TK, blockIdx);
     const int c3 = blockIdx.z;
     V *Uc = (V *)smem_raw;
     V *X = Uc + (size_t)nz * TK;
@@ -565,15 +566,19 @@ __global__ void __launch_bounds__(E::kColThreads, E::kMinBlocks) k_fused_vcomp(G
         if (c < t.nv) w[fidx<T>(g, k, t.ky, t.kx0 + c)] = Uc[idx];
     }
 }
+template <typename T, class E, int CTK = 0>
+__global__ void __launch_bounds__(E::kColThreads, E::kMinBlocks) k_fused_vcomp(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
+    fused_vcomp_body<T, E, CTK>(g, fd, a, TKrt, blockIdx);
+}
 
 // Split form, part 2: the projection of the three components written by k_fused_vcomp.
-template <typename T, class E, int CTK = 0>
-__global__ void __launch_bounds__(E::kColThreads, is_ff<T> ? 1 : 2) k_fused_vproj(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
+template <typename T, class E, int CTK>
+__device__ __forceinline__ void fused_vproj_body(const Geo &g, const typename E::Desc &fd, const FusedArgs &a, int TKrt, uint3 blockIdx) {
     const int TK = CTK ? CTK : TKrt;  // CTK: the tile width fixed at compile time, else 0
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nz = g.nz;
-    const ColTile t = col_tile<T>(g, TK);
+    const ColTile t = col_tile<T>(g, TK, blockIdx);
     const int tile = nz * TK;
     V *U = (V *)smem_raw;
     V *X = U + 3 * tile;
@@ -584,6 +589,10 @@ __global__ void __launch_bounds__(E::kColThreads, is_ff<T> ? 1 : 2) k_fused_vpro
     async_wait();
     __syncthreads();
     vel_project<T, E>(g, fd, a, t, U, X, Y, red, coef);
+}
+template <typename T, class E, int CTK = 0>
+__global__ void __launch_bounds__(E::kColThreads, is_ff<T> ? 1 : 2) k_fused_vproj(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
+    fused_vproj_body<T, E, CTK>(g, fd, a, TKrt, blockIdx);
 }
 
 // ----------------------------------------------------------------------------------------------
@@ -757,6 +766,20 @@ __global__ void __launch_bounds__(E::kColThreads, E::kMinBlocks) k_theta_herm(Ge
         if (c == 1 && kym == ky) continue;
         out[fidx<T>(g, k, c == 0 ? ky : kym, kx)] = R[E::pos(k, fd) * TK + c];
     }
+}
+
+// batched split velocity stage (batch.h): the two kernels over the tiles of several solvers
+template <typename T, class E>
+__global__ void __launch_bounds__(E::kColThreads, E::kMinBlocks) k_fused_vcomp_batch(const PassRec<E, FusedArgs> *recs, int n) {
+    uint3 bid;
+    const PassRec<E, FusedArgs> &r = batch_rec(recs, n, bid);
+    fused_vcomp_body<T, E, 0>(r.g, r.fd, r.a, r.tk, bid);
+}
+template <typename T, class E>
+__global__ void __launch_bounds__(E::kColThreads, is_ff<T> ? 1 : 2) k_fused_vproj_batch(const PassRec<E, FusedArgs> *recs, int n) {
+    uint3 bid;
+    const PassRec<E, FusedArgs> &r = batch_rec(recs, n, bid);
+    fused_vproj_body<T, E, 0>(r.g, r.fd, r.a, r.tk, bid);
 }
 
 }  // namespace sg

@@ -42,6 +42,17 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
                        : which == kFusedVComp  ? "fused_vcomp"
                        : which == kFusedVProj  ? "fused_vproj"
                                                : "theta_herm";
+    if (P.batch && (which == kFusedVComp || which == kFusedVProj)) {  // record (batch.h)
+        using R = PassRec<E, FusedArgs>;
+        const R r{{0, cdiv(P.nxh, tk), P.ny, which == kFusedVComp ? 3 : 1}, P.geo, fd, a.prepared(), tk};
+        if (which == kFusedVComp)
+            batch_add(*P.batch, r, (const void *)k_fused_vcomp_batch<T, E>,
+                      &batch_launch<R, k_fused_vcomp_batch<T, E>, E::kColThreads>, sm, name, bytes);
+        else
+            batch_add(*P.batch, r, (const void *)k_fused_vproj_batch<T, E>,
+                      &batch_launch<R, k_fused_vproj_batch<T, E>, E::kColThreads>, sm, name, bytes);
+        return OK;
+    }
     P.prof_begin(name, bytes);
     if (which == kFusedVelocity) {
         auto k = k_fused_velocity<T, E>;

@@ -14,6 +14,7 @@
 // E::pos(k) is the smem row that holds output k.
 #pragma once
 
+#include "batch.h"
 #include "fft.cuh"
 #include "fft4.cuh"
 #include "plan.h"
@@ -134,8 +135,8 @@ struct ZInvArgs {
     ZInvArgs prepared() const { ZInvArgs b = *this; b.scale_f = (float)scale; return b; }
 };
 
-template <typename T, class E, int CTK = 0>
-__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_inverse(Geo g, typename E::Desc fd, ZInvArgs a, int TKrt) {
+template <typename T, class E, int CTK>
+__device__ __forceinline__ void z_inverse_body(const Geo &g, const typename E::Desc &fd, const ZInvArgs &a, int TKrt, uint3 blockIdx) {
     const int TK = CTK ? CTK : TKrt;  // CTK: the tile width fixed at compile time, else 0
     const int lgTK = lg2(TK);
     using V = C2<T>;
@@ -181,6 +182,10 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_inverse(Geo g, ty
         }
         __syncthreads();
     }
+}
+template <typename T, class E, int CTK = 0>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_inverse(Geo g, typename E::Desc fd, ZInvArgs a, int TKrt) {
+    z_inverse_body<T, E, CTK>(g, fd, a, TKrt, blockIdx);
 }
 
 // ---------------------------------------------------------------------------------
@@ -294,7 +299,7 @@ struct YArgs {
 
 // CTK: the tile width when fixed at compile time, else 0 and the runtime TKrt
 template <typename T, class E, int CTK>
-__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass_t(Geo g, typename E::Desc fd, YArgs a, int TKrt) {
+__device__ __forceinline__ void y_pass_body(const Geo &g, const typename E::Desc &fd, const YArgs &a, int TKrt, uint3 blockIdx) {
     const int TK = CTK ? CTK : TKrt;
     const int lgTK = CTK ? (CTK == 16 ? 4 : CTK == 8 ? 3 : CTK == 4 ? 2 : CTK == 2 ? 1 : 0) : lg2(TKrt);
     using V = C2<T>;
@@ -338,6 +343,10 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass_t(Geo g, typ
         }
         __syncthreads();
     }
+}
+template <typename T, class E, int CTK>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass_t(Geo g, typename E::Desc fd, YArgs a, int TKrt) {
+    y_pass_body<T, E, CTK>(g, fd, a, TKrt, blockIdx);
 }
 
 // ---------------------------------------------------------------------------------
@@ -540,8 +549,8 @@ __host__ __device__ inline size_t x_nl_elems(const typename E::Desc &fd, int nxh
 // S while input t is transformed.
 // CRB: the rows per block when fixed at compile time (index arithmetic and the FFT's row offsets
 // become constants), else 0 and the runtime RBrt.
-template <typename T, class E, int CRB = 0>
-__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, typename E::Desc fd, XNLArgs a, int RBrt) {
+template <typename T, class E, int CRB>
+__device__ __forceinline__ void x_nonlinear_body(const Geo &g, const typename E::Desc &fd, const XNLArgs &a, int RBrt, uint3 blockIdx) {
     const int RB = CRB ? CRB : RBrt;
     const int lgRB = CRB ? (CRB == 16 ? 4 : CRB == 8 ? 3 : CRB == 4 ? 2 : CRB == 2 ? 1 : 0) : lg2(RBrt);
     using V = C2<T>;
@@ -609,6 +618,66 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, 
             }
         }
     }
+}
+template <typename T, class E, int CRB = 0>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, typename E::Desc fd, XNLArgs a, int RBrt) {
+    x_nonlinear_body<T, E, CRB>(g, fd, a, RBrt, blockIdx);
+}
+
+// ---------------------------------------------------------------------------------
+// Batched launches (batch.h): one launch runs the blocks of several solvers' launches of the
+// same kernel; flat block b belongs to the record with the largest block0 <= b, and runs the
+// kernel body with that record's arguments and its instance-local block index.
+// ---------------------------------------------------------------------------------
+template <class Rec>
+__device__ __forceinline__ const Rec &batch_rec(const Rec *recs, int n, uint3 &bid) {
+    int lo = 0, hi = n - 1;
+    const int b = (int)blockIdx.x;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (recs[mid].grid.block0 <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    const Rec &r = recs[lo];
+    const int l = b - r.grid.block0;
+    bid = make_uint3((unsigned)(l % r.grid.nbx), (unsigned)((l / r.grid.nbx) % r.grid.nby),
+                     (unsigned)(l / (r.grid.nbx * r.grid.nby)));
+    return r;
+}
+
+// the arguments of one pass launch (grid first: batch_add reads it)
+template <class E, class Args>
+struct PassRec {
+    BatchGrid grid;
+    Geo g;
+    typename E::Desc fd;
+    Args a;
+    int tk;
+};
+
+template <typename T, class E>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_z_inverse_batch(const PassRec<E, ZInvArgs> *recs, int n) {
+    uint3 bid;
+    const PassRec<E, ZInvArgs> &r = batch_rec(recs, n, bid);
+    z_inverse_body<T, E, 0>(r.g, r.fd, r.a, r.tk, bid);
+}
+template <typename T, class E>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_y_pass_batch(const PassRec<E, YArgs> *recs, int n) {
+    uint3 bid;
+    const PassRec<E, YArgs> &r = batch_rec(recs, n, bid);
+    y_pass_body<T, E, 0>(r.g, r.fd, r.a, r.tk, bid);
+}
+template <typename T, class E>
+__global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear_batch(const PassRec<E, XNLArgs> *recs, int n) {
+    uint3 bid;
+    const PassRec<E, XNLArgs> &r = batch_rec(recs, n, bid);
+    x_nonlinear_body<T, E, 0>(r.g, r.fd, r.a, r.tk, bid);
+}
+
+// host: the launch of a batched kernel over n records and `blocks` blocks in all
+template <class Rec, auto Kern, int NT>
+void batch_launch(const void *recs, int n, int blocks, size_t smem, cudaStream_t s) {
+    batch_launch_impl<Rec>(Kern, recs, n, blocks, smem, NT, s);
 }
 
 }  // namespace sg

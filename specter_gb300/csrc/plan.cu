@@ -1,6 +1,7 @@
 // Plan construction: the GB300 counterpart of fcgram_create_plan (src/fftp/fcgram_mod.f90:49-144,
 // tables :180-257) together with the grid / wavenumber setup the driver performs
 // (src/specter.fpp:683-800, kes module src/pseudo/pseudospec_mod.fpp:84-91).
+#include "batch.h"
 #include "plan.h"
 
 #include <cmath>
@@ -379,6 +380,7 @@ static cudaEvent_t take_event(Plan *p) {
 
 void Plan::prof_begin(const char *name, double bytes) {
     if (owner) { owner->prof_begin(name, bytes); return; }
+    if (batch) batch->unbatchable = name;  // a launch while recording: it has no batched form
     launches++;
     if (!profile) return;
     Rec r{name, bytes, take_event(this), take_event(this)};

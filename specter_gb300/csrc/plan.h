@@ -10,6 +10,8 @@
 
 namespace sg {
 
+struct Batch;  // batch.h
+
 // Plans are FP64 or FP32; FF (float-float) is the precision of internal tables and kernels of
 // the precision form on FP64 plans.
 enum Prec { FP64 = 0, FP32 = 1, FF = 2 };
@@ -75,6 +77,8 @@ struct Plan {
     // A companion plan (the FP32 plan of the nonlinear term of a mixed-precision solver) runs on
     // its owner's stream and counts and profiles its launches in its owner's records.
     Plan *owner = nullptr;
+    // while set, the batchable launchers record into it instead of launching (batch.h)
+    Batch *batch = nullptr;
     int nx = 0, ny = 0, nz = 0, cz = 0, oz = 0, nxh = 0, nzp = 0, ldx = 0, H = 0;
     double Lx = 1, Ly = 1, Lz = 1, Dkx = 1, Dky = 1, Dkz = 1, dz = 1;
     std::vector<double> kx, ky, kz, z, dir, fx, fy, fz;

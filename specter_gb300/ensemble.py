@@ -1,12 +1,15 @@
 """Batched ensemble of independent HD channel instances on one GPU.
 
-Each instance is its own plan and solver (uneven grids are allowed); the FP32-bulk solvers are
-autotuned per plan (tile-width caps, ``Solver.autotune``) and one RK step of all instances is
-captured as a single CUDA graph whose branches are the instances' plan streams, so that one
-graph launch advances the whole ensemble by one RK step and the instances' kernels overlap on
-the device.
+Each instance is its own plan and solver (uneven grids are allowed).  Two ways to run them:
 
-    python -m specter_gb300.ensemble --instances 64 --steps 200 --seq-sample 16
+* batch (default): ``api.Batch`` records one RK step of every FP32-bulk solver and replays it
+  as batched launches -- the i-th kernel of every instance's step runs as one launch per FFT
+  length class over the tiles of all the instances in that class -- captured as one CUDA graph
+  per RK step (a few dozen launches a step for the whole ensemble);
+* graph: the solvers are autotuned per plan and one RK step of all of them is captured as one
+  CUDA graph whose branches are the instances' own kernel chains (several hundred kernels).
+
+    python -m specter_gb300.ensemble --instances 64 --steps 200 [--mode graph] [--seq-sample K]
 
 Instance draw (seeded, numpy PCG64): nx, ny in {32, 48, 64, 96}, nz (physical) in {33, 65, 97}
 (+25 FC-Gram points), z in [0, 2], nu log-uniform in [2e-4, 2e-3], RK2, dt = 1e-4, and the
@@ -54,7 +57,7 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a))
 
 
-def run(instances=64, steps=200, seed=20261203, seq_sample=None, autotune=True, graph_steps=1):
+def run(instances=64, steps=200, seed=20261203, seq_sample=None, autotune=True, graph_steps=1, mode="batch"):
     from specter_gb300 import api, initial
     insts = draw(instances, seed)
     t0 = time.perf_counter()
@@ -62,29 +65,37 @@ def run(instances=64, steps=200, seed=20261203, seq_sample=None, autotune=True, 
     t_build = time.perf_counter() - t0
     caps = []
     t0 = time.perf_counter()
-    for _, s in built:
-        caps.append(s.autotune() if autotune else None)
-    t_tune = time.perf_counter() - t0
     solvers = [s for _, s in built]
-    if steps % graph_steps:
-        raise ValueError("steps must be a multiple of graph_steps")
-    graph = api.Graph(solvers, nsteps=graph_steps)
+    if mode == "batch":
+        runner = api.Batch(solvers)
+        kernels = runner.kernels
+    else:
+        for _, s in built:
+            caps.append(s.autotune() if autotune else None)
+        if steps % graph_steps:
+            raise ValueError("steps must be a multiple of graph_steps")
+        runner = api.Graph(solvers, nsteps=graph_steps)
+        kernels = runner.kernels // graph_steps
+    t_prep = time.perf_counter() - t0
     for p, _ in built:
         p.synchronize()
     t0 = time.perf_counter()
-    for _ in range(steps // graph_steps):
-        graph.launch()
-    graph.synchronize()
+    if mode == "batch":
+        runner.step(steps)
+    else:
+        for _ in range(steps // graph_steps):
+            runner.launch()
+    runner.synchronize()
     t_run = time.perf_counter() - t0
     for s in solvers:
         s.check()
     solves_per_s = instances / t_run
     pts = sum(x["nx"] * x["ny"] * x["nzp"] * x["ord"] for x in insts) * steps
-    result = {"instances": instances, "steps": steps, "seed": seed, "precision": "fp32-bulk",
-              "graph_steps": graph_steps, "graph_kernels_per_step": graph.kernels // graph_steps,
-              "seconds": round(t_run, 4),
+    result = {"instances": instances, "steps": steps, "seed": seed, "precision": "fp32-bulk", "mode": mode,
+              "kernels_per_step": kernels, "seconds": round(t_run, 4),
               "solves_per_s": round(solves_per_s, 3), "mpts_stages_per_s": round(pts / t_run / 1e6, 2),
-              "build_s": round(t_build, 2), "autotune_s": round(t_tune, 2), "caps": caps}
+              "build_s": round(t_build, 2), "prepare_s": round(t_prep, 2), "caps": caps or None}
+    graph = runner
     # sequential plain FP64 on a sample (first k instances): time per solve, error of the ensemble
     k = instances if seq_sample is None else min(seq_sample, instances)
     if k > 0:
@@ -127,11 +138,14 @@ def main(argv=None):
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--seed", type=int, default=20261203)
-    ap.add_argument("--seq-sample", type=int, default=None, help="instances run through sequential FP64")
+    ap.add_argument("--seq-sample", type=int, default=None,
+                    help="instances run through sequential FP64 (default: all of them)")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--graph-steps", type=int, default=1, help="RK steps captured per graph launch")
+    ap.add_argument("--graph-steps", type=int, default=1, help="RK steps captured per graph launch (mode graph)")
+    ap.add_argument("--mode", default="batch", choices=("batch", "graph"))
     args = ap.parse_args(argv)
-    res, _, _ = run(args.instances, args.steps, args.seed, args.seq_sample, not args.no_autotune, args.graph_steps)
+    res, _, _ = run(args.instances, args.steps, args.seed, args.seq_sample, not args.no_autotune, args.graph_steps,
+                    args.mode)
     print(json.dumps(res), flush=True)
     return res
 
