@@ -23,7 +23,8 @@ struct BatchGrid {
     int block0, nbx, nby, nbz;
 };
 
-typedef void (*BatchLaunchFn)(const void *recs, int n, int blocks, size_t smem, cudaStream_t s);
+// setup_only: set the kernel's shared-memory limit and return (done before stream capture)
+typedef void (*BatchLaunchFn)(const void *recs, int n, int blocks, size_t smem, cudaStream_t s, bool setup_only);
 
 struct BatchEntry {
     const void *key;                 // the batched kernel: entries with the same key and smem share a launch
@@ -41,8 +42,12 @@ struct Batch {
 };
 
 template <class Rec, class Kern>
-void batch_launch_impl(Kern kern, const void *recs, int n, int blocks, size_t smem, int threads, cudaStream_t s) {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+void batch_launch_impl(Kern kern, const void *recs, int n, int blocks, size_t smem, int threads, cudaStream_t s,
+                       bool setup_only) {
+    if (setup_only) {  // always: the kernel's static shared memory counts against the default 48 KB too
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        return;
+    }
     kern<<<blocks, threads, smem, s>>>((const Rec *)recs, n);
 }
 

@@ -1,4 +1,5 @@
 // C ABI (include/specter_gpu.h): handles, reference-layout conversion, dispatch on precision.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -1029,19 +1030,40 @@ int specter_batch_create(specter_solver *const *solvers, int n, specter_batch **
     }
     cudaMemcpy(b->recs, host.data(), host.size(), cudaMemcpyHostToDevice);
     cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    // the shared-memory limit is a per-kernel attribute: set each kernel's largest use once (a
+    // kernel appears at several positions with different tile sizes)
+    std::vector<std::pair<const BatchEntry *, size_t>> limits;
+    for (const Group &g : seq) {
+        bool found = false;
+        for (auto &l : limits)
+            if (l.first->key == g.proto->key) { l.second = std::max(l.second, g.proto->smem); found = true; }
+        if (!found) limits.push_back({g.proto, g.proto->smem});
+    }
+    for (auto &l : limits) l.first->launch(nullptr, 0, 0, l.second, b->stream, true);
+    if ((st = check_launch("batch kernel attributes"))) {
+        specter_batch_destroy(b);
+        return st;
+    }
     if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
         st = check_launch("batch capture");
         specter_batch_destroy(b);
         return st ? st : SPECTER_ERR_CUDA;
     }
     for (const Group &g : seq) {
-        g.proto->launch((const unsigned char *)b->recs + g.off, g.n, g.blocks, g.proto->smem, b->stream);
+        g.proto->launch((const unsigned char *)b->recs + g.off, g.n, g.blocks, g.proto->smem, b->stream, false);
         b->kernels++;
+        const cudaError_t el = cudaPeekAtLastError();
+        if (el != cudaSuccess && !st) {
+            set_error(std::string("batch capture: ") + g.proto->name + " (" + std::to_string(g.n) + " instances, " +
+                      std::to_string(g.blocks) + " blocks, " + std::to_string(g.proto->smem) + " B smem): " +
+                      cudaGetErrorString(el));
+            st = SPECTER_ERR_CUDA;
+        }
     }
     cudaGraph_t graph = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(b->stream, &graph);
     b->graph = graph;
-    if (ec != cudaSuccess) { set_error(std::string("batch capture: ") + cudaGetErrorString(ec)); st = SPECTER_ERR_CUDA; }
+    if (ec != cudaSuccess && !st) { set_error(std::string("batch capture: ") + cudaGetErrorString(ec)); st = SPECTER_ERR_CUDA; }
     if (!st && cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess) {
         set_error("batch graph instantiation failed");
         st = SPECTER_ERR_CUDA;

@@ -676,8 +676,8 @@ __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear_batch(c
 
 // host: the launch of a batched kernel over n records and `blocks` blocks in all
 template <class Rec, auto Kern, int NT>
-void batch_launch(const void *recs, int n, int blocks, size_t smem, cudaStream_t s) {
-    batch_launch_impl<Rec>(Kern, recs, n, blocks, smem, NT, s);
+void batch_launch(const void *recs, int n, int blocks, size_t smem, cudaStream_t s, bool setup_only) {
+    batch_launch_impl<Rec>(Kern, recs, n, blocks, smem, NT, s, setup_only);
 }
 
 }  // namespace sg

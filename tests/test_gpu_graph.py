@@ -85,8 +85,9 @@ def test_graph_query_and_memory():
     g.close()
 
 
-def test_small_ensemble_run():
+@pytest.mark.parametrize("mode", ["batch", "graph"])
+def test_small_ensemble_run(mode):
     from specter_gb300 import ensemble
-    res, insts, built = ensemble.run(instances=4, steps=5, seed=11, seq_sample=2)
-    assert res["solves_per_s"] > 0 and res["graph_kernels_per_step"] > 0
+    res, insts, built = ensemble.run(instances=4, steps=5, seed=11, seq_sample=2, mode=mode)
+    assert res["solves_per_s"] > 0 and res["kernels_per_step"] > 0
     assert res["fp32_vs_fp64_rel_l2_max"] < 1e-5
