@@ -1,6 +1,6 @@
 // Float-float ("double-word") arithmetic on the FP32 pipes.
 //
-// A value is the unevaluated sum hi + lo of two floats with |lo| <= ulp(hi) / 2: about 48
+// A value is the unevaluated sum hi + lo of two floats with |lo| at most a few ulp(hi): about 48
 // significant bits.  GB300 executes FP64 at 1/64 of its FP32 rate, so the column kernels of the
 // precision form, which need more than FP32 (the FC-Gram continuation amplifies rounding in the
 // wall-adjacent rows by up to 1e4), compute in this format instead of FP64.
@@ -9,8 +9,9 @@
 // Fast2Sum (Dekker 1971), and the FMA-based exact product; the compositions follow Joldes,
 // Muller and Popescu, "Tight and rigorous error bounds for basic building blocks of
 // double-word arithmetic" (ACM TOMS 44, 2017):
-//   add  (their SloppyDWPlusDW, 11 flops): error <= ~3 u^2 (|a| + |b|), u = 2^-24 -- a
-//        normwise bound, which is what FFT butterflies and sums need;
+//   add  (their SloppyDWPlusDW without its final renormalisation, 8 flops): error
+//        <= ~3 u^2 (|a| + |b|), u = 2^-24 -- a normwise bound, which is what FFT butterflies
+//        and sums need;
 //   mul  (DWTimesDW with FMAs, 7 flops):   relative error <= ~5 u^2;
 //   by a float (DWTimesFP, 6 flops).
 // Nothing here relies on reassociation: nvcc keeps IEEE order without --use_fast_math, and the
@@ -54,13 +55,13 @@ __device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &
     e = b - (s - a);
 }
 
+// Sums leave the pair unnormalised (|lo| may grow to a few ulp(hi) along a chain of additions):
+// the leading words' rounding is still captured exactly by TwoSum, lo's own rounding is
+// 2^-24 |lo|, and the products renormalise.  8 flops instead of 11.
 __device__ __forceinline__ ff ff_add(ff a, ff b) {
     float s, e;
     two_sum(a.hi, b.hi, s, e);
-    e += a.lo + b.lo;
-    float h, l;
-    fast_two_sum(s, e, h, l);
-    return ff(h, l);
+    return ff(s, e + (a.lo + b.lo));
 }
 __device__ __forceinline__ ff ff_neg(ff a) { return ff(-a.hi, -a.lo); }
 __device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }

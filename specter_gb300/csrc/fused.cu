@@ -75,11 +75,12 @@ __global__ void k_q2d(const ffc *src, double2 *dst, size_t n) {
         dst[q] = make_double2(ff_to_double(v.x), ff_to_double(v.y));
     }
 }
-// FP32 copy of a float-float field (its leading parts): the nonlinear term's input
+// FP32 copy of a float-float field: the nonlinear term's input.  The pairs may be unnormalised
+// (ff.cuh), so the copy is the rounded sum of both words, not the leading word.
 __global__ void k_q2f(const ffc *src, float2 *dst, size_t n) {
     for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
         const float4 v = *(const float4 *)(src + q);
-        dst[q] = make_float2(v.x, v.z);
+        dst[q] = make_float2(v.x + v.y, v.z + v.w);
     }
 }
 
