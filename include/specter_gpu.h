@@ -192,7 +192,9 @@ int specter_plan_tile_caps(specter_plan *plan, const int caps[4]);
 /* named plan options: "velocity_split" (0/1: fused velocity stage as one kernel or as a
  * per-component kernel plus a projection kernel), "tile_cap_z|y|x|fused" (1, 2, 4, 8, 16),
  * "ff_threads" (256 or 384: threads per block of the float-float column kernels of nl_fp32
- * solvers; the autotuner picks it for those solvers) */
+ * solvers on the generic transform engine; the autotuner picks it for those solvers),
+ * "ff_engine" (1, the default: those kernels use the three-step register Bluestein engine when
+ * nz + C lies in (270, 540]; 0: always the generic engine) */
 int specter_plan_set_option(specter_plan *plan, const char *name, int value);
 int specter_graph_create(specter_solver *const *solvers, int n, int nsteps, specter_graph **out);
 int specter_graph_launch(specter_graph *g);

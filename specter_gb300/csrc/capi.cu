@@ -668,6 +668,7 @@ int specter_plan_set_option(specter_plan *plan, const char *name, int value) {
     if (!name) { set_error("null option name"); return SPECTER_ERR_ARG; }
     Plan &P = *plan->p;
     if (!strcmp(name, "velocity_split")) { P.velocity_split = value ? 1 : 0; return SPECTER_OK; }
+    if (!strcmp(name, "ff_engine")) { P.ff_engine = value ? 1 : 0; return SPECTER_OK; }
     if (!strcmp(name, "ff_threads")) {
         if (value != 256 && value != 384) { set_error("ff_threads is 256 or 384"); return SPECTER_ERR_ARG; }
         P.ff_threads = value;

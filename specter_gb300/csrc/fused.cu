@@ -23,6 +23,7 @@ struct FusedState {
     // (vq, prq) held in float-float inside the RK loop (converted from and to the FP64 fields at
     // the ends of fused_step / fused_stage; cq: the RK step start for fused_stage)
     FFTTable tzq;
+    FFBTable ffb;  // the three-step float-float engine's tables, when the z length has them
     void *vq[4] = {nullptr, nullptr, nullptr, nullptr};
     void *cq[4] = {nullptr, nullptr, nullptr, nullptr};
     void *prq = nullptr;
@@ -184,10 +185,16 @@ int fused_create(Plan &P, const StageParams &sp, FusedState **out) {
             ok = ok && cudaMalloc(&fs->cq[i], P.field_bytes()) == cudaSuccess;
         }
         ok = ok && cudaMalloc(&fs->prq, P.field_bytes()) == cudaSuccess;
-        if (ok && build_fft_table(fs->tzq, P.nz, FF)) {
-            fused_destroy(fs);
-            set_error("float-float FFT table construction failed");
-            return ERR_CUDA;
+        if (ok) {
+            if (const int st2 = build_ffb_table(fs->ffb, P.nz)) {
+                fused_destroy(fs);
+                return st2;
+            }
+            if (build_fft_table(fs->tzq, P.nz, FF)) {
+                fused_destroy(fs);
+                set_error("float-float FFT table construction failed");
+                return ERR_CUDA;
+            }
         }
     }
     if (!ok) {
@@ -244,6 +251,7 @@ void fused_destroy(FusedState *fs) {
     }
     if (fs->prq) cudaFree(fs->prq);
     free_fft_table(fs->tzq);
+    free_ffb_table(fs->ffb);
     if (fs->nlp) plan_destroy(fs->nlp);
     delete fs;
 }
@@ -251,10 +259,9 @@ void fused_destroy(FusedState *fs) {
 template <typename T>
 static int launch(Plan &P, const FusedState *fs, const FusedArgs &a, int which, double bytes) {
     if constexpr (is_ff<T>) {
-        // the generic Stockham engine: in float-float its radix-8/5/3 butterflies with their
-        // trivial rotations done as swaps take fewer float-float multiplies than register DFTs
-        // of 8, 9 and 15 points with table twiddles (three passes instead of five: measured
-        // 30 % slower at 512^2 x 513)
+        // the three-step register engine where the z length has its tables (2.6x the generic
+        // engine's transform rate at n = 538), else the generic Stockham engine
+        if (fs->ffb.ok && P.ff_engine) return ffb_fused(P, fs->ffb.d, a, which, bytes);
         if (P.ff_threads == 256) return launch_fused<ff, GenericFFT<ff, 256>>(P, fs->tzq.d, a, which, bytes);
         return launch_fused<ff, GenericFFT<ff, 384>>(P, fs->tzq.d, a, which, bytes);
     } else {

@@ -3,6 +3,7 @@
 
 #include <string>
 
+#include "ffblue.cuh"
 #include "fused_kernels.cuh"
 
 namespace sg {
@@ -85,5 +86,17 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
 
 // four-step variant (fused_fast_f32.cu); kNoFast (-1) when the plan has no four-step z table
 int fast_fused(Plan &P, const FusedArgs &a, int which, double bytes);
+
+// tables of the float-float three-step Bluestein engine (ffblue.cuh) for one z length;
+// ok == 0 when the length is outside (L/4, L/2] and the generic engine serves it (fused_ffb.cu)
+struct FFBTable {
+    FFBDesc d{};
+    void *mem = nullptr;
+    int ok = 0;
+};
+int build_ffb_table(FFBTable &t, int n);
+void free_ffb_table(FFBTable &t);
+// the float-float column kernels on that engine (fused_ffb.cu)
+int ffb_fused(Plan &P, const FFBDesc &d, const FusedArgs &a, int which, double bytes);
 
 }  // namespace sg

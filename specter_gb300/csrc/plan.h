@@ -113,8 +113,12 @@ struct Plan {
     int tile_cap[4] = {16, 16, 16, 16};
     // fused velocity stage as two kernels (per-component update, then the projection) or one
     int velocity_split = 1;
-    // threads per block of the float-float column kernels (nl_fp32 form): 256 or 384
+    // threads per block of the float-float column kernels (nl_fp32 form) on the generic
+    // engine: 256 or 384
     int ff_threads = 384;
+    // float-float column kernels: 1 = the three-step Bluestein engine (ffblue.cuh) where the z
+    // length has one, 0 = always the generic engine
+    int ff_engine = 1;
     int capped(int t, int kind) const { return t < tile_cap[kind] ? t : tile_cap[kind]; }
     long long launches = 0;
     bool profile = false;

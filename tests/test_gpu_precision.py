@@ -79,6 +79,51 @@ def test_nl_fp32_bouss_nz538(convection):
     assert e[3] < 1e-9
 
 
+@pytest.mark.parametrize("split", [1, 0], ids=["split", "one_kernel"])
+def test_nl_fp32_engines_agree(convection, split):
+    """The float-float column kernels on the three-step Bluestein engine (the default at this z
+    length) and on the generic Stockham engine: the same arithmetic up to float-float rounding
+    (~1e-14 per transform), in the split velocity form and in the one-kernel form (whose tile
+    widths and thread counts differ).  Compared as spectra, where the FC-Gram continuation
+    rows carry the wall-adjacent rounding amplified ~1e4x: after 20 steps both held to 1e-9
+    (the physical-grid errors against the oracle stay at 1e-11)."""
+    from specter_gb300 import api
+    plan, g, ref, run = convection
+    outs = []
+    for engine in (1, 0):
+        api.set_option(plan, "ff_engine", engine)
+        api.set_option(plan, "velocity_split", split)
+        outs.append(run(fused=True, nl_fp32=True))
+    api.set_option(plan, "ff_engine", 1)
+    api.set_option(plan, "velocity_split", 1)
+    d = [rel(a, b) for a, b in zip(outs[0][:4], outs[1][:4])]
+    print("engines after %d steps (split %d): vx %.2e vy %.2e vz %.2e th %.2e" % (STEPS, split, *d))
+    assert max(d) < 1e-9
+    e = _errors(g, outs[0], ref)
+    assert max(e[:3]) < 5e-6 and e[3] < 1e-9
+
+
+def test_nl_fp32_channel_nz282():
+    """The channel z length of the 256^2 x 257 precision case (nz + C = 282 = 2 * 3 * 47, on the
+    three-step engine as well): 16 x 16 x 257, Lz = 2, RK4, 20 steps against the oracle."""
+    from specter_gb300 import api, initial
+    plan, g = make_pair(16, 16, 257, 2.0)
+    real = initial.channel_velocity(plan, seed=SEED, amp=0.1, kmax=4)
+    v0 = [g.fftp3d_real_to_complex(r) for r in real]
+    pr0 = np.zeros(g.sshape, complex)
+    kw = dict(dt=2e-5, nu=2e-4, ord=4)
+    ref = g.run(g.params(**kw), 20, *v0, pr0)
+    s = api.Solver(plan, api.HD, fused=True, nl_fp32=True, **kw)
+    for f, a in zip((s.vx, s.vy, s.vz, s.pr), v0 + [pr0]):
+        f.upload(a)
+    s.step(20)
+    got = [f.download() for f in (s.vx, s.vy, s.vz)]
+    s.close()
+    e = [rel(a, b) for a, b in zip(got, ref[:3])]
+    print("nl_fp32 channel nz 282 vs oracle after 20 steps: %.2e %.2e %.2e" % tuple(e))
+    assert max(e) < 1e-7
+
+
 def test_nl_fp32_channel():
     """The plain channel configuration (64 x 64 x 65, 100 RK2 steps) in the precision form."""
     from specter_gb300 import api, initial
