@@ -311,6 +311,8 @@ def main():
     ap.add_argument("--grid", default=None, help="NX,NY,NZP: another grid of the same case (profiling, sweeps)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default tile widths")
     ap.add_argument("--caps", default=None, help="Z,Y,X,FUSED,SPLIT: set these instead of autotuning")
+    ap.add_argument("--ff", default=None, help="PAIR_PROJ,PAIR_COLS: block shapes of the float-float column kernels "
+                                                 "(with --caps; 0 = one 576-thread block per SM, 1 = two of 288)")
     ap.add_argument("--form", default="nl32", choices=sorted(FORMS),
                     help="the timed form: nl32 (the precision form, default), fp32 (FP32-bulk), fp64 (plain)")
     ap.add_argument("--fp64", action="store_true", help="same as --form fp64")
@@ -348,8 +350,12 @@ def main():
         caps = [int(v) for v in args.caps.split(",")]
         api.set_tile_caps(plan, caps[:4])
         api.set_option(plan, "velocity_split", caps[4])
+        if args.ff:
+            for name, v in zip(("ff_pair_proj", "ff_pair_cols"), args.ff.split(",")):
+                api.set_option(plan, name, int(v))
     else:
         caps = s.autotune() if not args.no_autotune else None
+    ff_opts = {n: api.get_option(plan, n) for n in ("ff_engine", "ff_pair_proj", "ff_pair_cols")} if form == "nl32" else None
     for _ in range(W):
         s.step(1)
     plan.synchronize()
@@ -413,6 +419,7 @@ def main():
                            "form": form, "form_detail": FORMS[form],
                            "path": "reference-sequence" if args.refseq else "fused",
                            "autotune_caps_z_y_x_fused_split": list(caps) if caps else None,
+                           "ff_column_kernels": ff_opts,
                            "l2": f"inputs larger than L2 ({field_mb:.0f} MB per field), no flush",
                            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
                 "roofline": roof,

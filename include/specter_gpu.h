@@ -194,8 +194,12 @@ int specter_plan_tile_caps(specter_plan *plan, const int caps[4]);
  * "ff_threads" (256 or 384: threads per block of the float-float column kernels of nl_fp32
  * solvers on the generic transform engine; the autotuner picks it for those solvers),
  * "ff_engine" (1, the default: those kernels use the three-step register Bluestein engine when
- * nz + C lies in (270, 540]; 0: always the generic engine) */
+ * nz + C lies in (270, 540]; 0: always the generic engine), "ff_pair_proj" and "ff_pair_cols"
+ * (0/1: on that engine, the projection kernel and the other column kernels run as one 576-thread
+ * block per SM or as two 288-thread blocks; the autotuner picks them) */
 int specter_plan_set_option(specter_plan *plan, const char *name, int value);
+/* the current value of a named plan option (the names above); no reference counterpart */
+int specter_plan_get_option(specter_plan *plan, const char *name, int *value);
 int specter_graph_create(specter_solver *const *solvers, int n, int nsteps, specter_graph **out);
 int specter_graph_launch(specter_graph *g);
 int specter_graph_synchronize(specter_graph *g);

@@ -31,7 +31,7 @@ EXPORTS = [
     "specter_s_imposebc",
     "specter_solver_create", "specter_solver_destroy", "specter_solver_fields", "specter_solver_step",
     "specter_solver_stage", "specter_solver_check",
-    "specter_solver_autotune", "specter_plan_tile_caps", "specter_plan_set_option",
+    "specter_solver_autotune", "specter_plan_tile_caps", "specter_plan_set_option", "specter_plan_get_option",
     "specter_graph_create", "specter_graph_launch", "specter_graph_synchronize", "specter_graph_kernels",
     "specter_graph_destroy", "specter_graph_query", "specter_solver_memory", "specter_device_memory",
     "specter_table_check", "specter_fields_upload", "specter_fields_download",
@@ -93,6 +93,7 @@ def load(path: str | None = None):
     L.specter_solver_autotune.argtypes = [VP, C.POINTER(C.c_int)]
     L.specter_plan_tile_caps.argtypes = [VP, C.POINTER(C.c_int)]
     L.specter_plan_set_option.argtypes = [VP, C.c_char_p, C.c_int]
+    L.specter_plan_get_option.argtypes = [VP, C.c_char_p, C.POINTER(C.c_int)]
     L.specter_graph_create.argtypes = [C.POINTER(VP), C.c_int, C.c_int, C.POINTER(VP)]
     L.specter_graph_launch.argtypes = [VP]
     L.specter_graph_synchronize.argtypes = [VP]

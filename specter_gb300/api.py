@@ -419,6 +419,13 @@ def set_option(plan: Plan, name: str, value: int):
     check(_L(plan).specter_plan_set_option(plan.h, name.encode(), int(value)))
 
 
+def get_option(plan: Plan, name: str) -> int:
+    """Current value of a named plan option (specter_plan_get_option)."""
+    v = C.c_int()
+    check(_L(plan).specter_plan_get_option(plan.h, name.encode(), C.byref(v)))
+    return v.value
+
+
 def set_tile_caps(plan: Plan, caps):
     """Tile-width caps (z, y, x, fused) of the plan's kernels; entries <= 0 are left unchanged."""
     c = (C.c_int * 4)(*caps)

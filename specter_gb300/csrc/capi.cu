@@ -669,6 +669,8 @@ int specter_plan_set_option(specter_plan *plan, const char *name, int value) {
     Plan &P = *plan->p;
     if (!strcmp(name, "velocity_split")) { P.velocity_split = value ? 1 : 0; return SPECTER_OK; }
     if (!strcmp(name, "ff_engine")) { P.ff_engine = value ? 1 : 0; return SPECTER_OK; }
+    if (!strcmp(name, "ff_pair_proj")) { P.ff_pair_proj = value ? 1 : 0; return SPECTER_OK; }
+    if (!strcmp(name, "ff_pair_cols")) { P.ff_pair_cols = value ? 1 : 0; return SPECTER_OK; }
     if (!strcmp(name, "ff_threads")) {
         if (value != 256 && value != 384) { set_error("ff_threads is 256 or 384"); return SPECTER_ERR_ARG; }
         P.ff_threads = value;
@@ -681,6 +683,20 @@ int specter_plan_set_option(specter_plan *plan, const char *name, int value) {
             P.tile_cap[i] = value;
             return SPECTER_OK;
         }
+    set_error(std::string("unknown plan option ") + name);
+    return SPECTER_ERR_ARG;
+}
+
+int specter_plan_get_option(specter_plan *plan, const char *name, int *value) {
+    CHECK_PLAN(plan);
+    if (!name || !value) { set_error("null argument"); return SPECTER_ERR_ARG; }
+    const Plan &P = *plan->p;
+    const struct { const char *n; int v; } opts[] = {
+        {"velocity_split", P.velocity_split}, {"ff_threads", P.ff_threads}, {"ff_engine", P.ff_engine},
+        {"ff_pair_proj", P.ff_pair_proj},     {"ff_pair_cols", P.ff_pair_cols}, {"tile_cap_z", P.tile_cap[0]},
+        {"tile_cap_y", P.tile_cap[1]},        {"tile_cap_x", P.tile_cap[2]},   {"tile_cap_fused", P.tile_cap[3]}};
+    for (const auto &o : opts)
+        if (!strcmp(name, o.n)) { *value = o.v; return SPECTER_OK; }
     set_error(std::string("unknown plan option ") + name);
     return SPECTER_ERR_ARG;
 }
@@ -727,13 +743,16 @@ int specter_solver_autotune(specter_solver *s, int caps[5]) {
         if (!(ms_other < ms_keep)) P.velocity_split = keep;
         st = snap.put_back(s);
     }
-    if (!st && s->fused && s->sp.nl_fp32) {  // block size of the float-float column kernels
-        const int keep = P.ff_threads;
-        const float ms_keep = trial();
-        P.ff_threads = keep == 384 ? 256 : 384;
-        const float ms_other = trial();
-        if (!(ms_other < ms_keep)) P.ff_threads = keep;
-        st = snap.put_back(s);
+    if (!st && s->fused && s->sp.nl_fp32) {  // block shapes of the float-float column kernels
+        int *opt[3] = {&P.ff_threads, &P.ff_pair_proj, &P.ff_pair_cols};
+        for (int i = 0; i < 3 && !st; i++) {
+            const int keep = *opt[i];
+            const float ms_keep = trial();
+            *opt[i] = i == 0 ? (keep == 384 ? 256 : 384) : !keep;
+            const float ms_other = trial();
+            if (!(ms_other < ms_keep)) *opt[i] = keep;
+            st = snap.put_back(s);
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -341,12 +341,14 @@ __device__ __noinline__ void run_out(Q *X, const Q *tab, int n, int sign) {
 
 // Engine interface of the fused column kernels (kernels.cuh: GenericFFT, FourStep) for the
 // float-float kernels on this transform: one in-place buffer, natural order in and out, tables
-// through the read-only cache (measured as fast as staging them in shared memory), NT threads.
-template <int NT>
+// through the read-only cache (measured as fast as staging them in shared memory), NT threads,
+// MINB blocks per SM.
+template <int NT, int MINB = 1>
 struct FFBlue {
     using Desc = FFBDesc;
     static constexpr int kBuffers = 1;
-    static constexpr int kMinBlocks = 1;
+    static constexpr bool kStreamProj = true;  // the projection without staged components
+    static constexpr int kMinBlocks = MINB;
     static constexpr int kColThreads = NT;
     static constexpr int kWideThreads = NT;
     static int wide_threads(int) { return NT; }

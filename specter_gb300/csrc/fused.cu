@@ -315,6 +315,8 @@ static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], c
         a.vout[i] = vout[i];
     }
     a.pr = pr;
+    if constexpr (is_ff<T>)
+        if (fs->nlp && fs->nlp->tz4.ok && fs->ffb.ok && P.ff_engine) a.z32 = fs->nlp->tz4.d;
     a.side = fs->side;
     a.hspec[0] = fs->E[0];
     a.hspec[1] = fs->E[1];

@@ -83,10 +83,19 @@ void free_ffb_table(FFBTable &t) {
     t = FFBTable{};
 }
 
-// 576 threads: at a tile width of 8 the three steps have 1080, 576 and 960 items (two rounds,
-// one, two), and the kernels stay at one block of 18 warps per SM
+// Two block shapes, chosen per kernel family by the plan (the autotuner tries both):
+//   one block of 576 threads per SM at a tile width of 8: the three transform steps have 1080,
+//   576 and 960 items (two rounds, one, two); alone the transform is fastest so (26 ns a column
+//   against 29 ns for the pair below);
+//   two blocks of 288 threads per SM at a width of 4: the same items per thread, and one block's
+//   global loads and barriers overlap the other's arithmetic.
+// Copies of the column kernels with the width fixed carry one transform body each.
 int ffb_fused(Plan &P, const FFBDesc &d, const FusedArgs &a, int which, double bytes) {
-    return launch_fused<ff, FFBlue<576>>(P, d, a, which, bytes);
+    // the projection's FP32 pressure transform uses this translation unit's constant twiddles
+    if (fft4_ensure_tables() != cudaSuccess) { set_error("constant table upload failed"); return ERR_CUDA; }
+    const bool pair = which == kFusedVProj ? P.ff_pair_proj : P.ff_pair_cols;
+    if (pair) return launch_fused<ff, FFBlue<288, 2>, 4>(P, d, a, which, bytes);
+    return launch_fused<ff, FFBlue<576>, 8>(P, d, a, which, bytes);
 }
 
 }  // namespace sg

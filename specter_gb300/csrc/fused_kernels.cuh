@@ -41,6 +41,8 @@ struct FusedArgs {
     int nl32;             // the NL fields are FP32 (nl_fp32 form) while the kernel runs in FP64
     int nl_spec;          // (with nl32) the NL fields are already z spectra: rows [0, nz), the
                           // forward transform with continuation done by the FP32 pipeline
+    FFT4Desc z32;         // nl_fp32 on the three-step float-float engine: the FP32 companion plan's
+                          // four-step z tables, for the pressure potential's bulk rows (L1 = 0: none)
     float f_dt, f_nu, f_kappa, f_rmp, f_xmom, f_xtemp, f_wall_tmp, f_omega[3];  // FP32 mirrors
     ff q_dt, q_nu, q_kappa, q_rmp, q_xmom, q_xtemp, q_wall_tmp, q_omega[3];      // float-float
     FusedArgs prepared() const {
@@ -189,13 +191,24 @@ __device__ __forceinline__ void nl_tile_load(C2<T> *dst, const FusedArgs &a, int
                                              int TK, int nv) {
     if constexpr (!is_f32<T>) {
         if (a.nl32) {
+            // eight loads per thread in flight before the converting stores (one at a time, each
+            // waited for in turn, they left the SM idle for most of the load phase)
             const float2 *src = (const float2 *)a.nl[c] + col0;
-            const int lgTK = lg2(TK);
-            for (int idx = threadIdx.x; idx < rows * TK; idx += blockDim.x) {
-                const int k = idx >> lgTK, cc = idx & (TK - 1);
-                float2 f = make_float2(0.f, 0.f);
-                if (cc < nv) f = __ldg(src + ((unsigned)k * zs + (unsigned)cc));
-                dst[idx] = from_f2<T>(f);
+            const int lgTK = lg2(TK), total = rows * TK;
+            for (int base = threadIdx.x; base < total; base += 8 * blockDim.x) {
+                float2 f[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int idx = base + u * blockDim.x;
+                    const int k = idx >> lgTK, cc = idx & (TK - 1);
+                    f[u] = make_float2(0.f, 0.f);
+                    if (idx < total && cc < nv) f[u] = __ldg(src + ((unsigned)k * zs + (unsigned)cc));
+                }
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int idx = base + u * blockDim.x;
+                    if (idx < total) dst[idx] = from_f2<T>(f[u]);
+                }
             }
             async_commit();
             return;
@@ -495,6 +508,185 @@ __device__ void vel_project(const Geo &g, const typename E::Desc &fd, const Fuse
     }
 }
 
+// The pressure potential's bulk rows through the FP32 four-step engine of the companion plan:
+// pr is an output no later stage reads except at its two wall rows, which come from float-float
+// sums over the spectrum (exact like the transform's).  The bulk rows then carry FP32 rounding,
+// as their FP32 exponential profile already does.  L1 x L2: the compiled FP32 z splits of the
+// lengths this engine serves (1080 = 36 x 30 for nz + C = 538, 576 = 24 x 24 for 282).
+template <int L1, int L2>
+__device__ __forceinline__ void pressure_fp32(float2 *X32, int TK, const FFT4Desc &d) {
+    FourStep<float, L1, L2, true>::run(X32, nullptr, TK, d, +1);
+}
+__device__ __forceinline__ bool pressure_fp32_ok(const FFT4Desc &d) {
+    return d.blue && ((d.L1 == 36 && d.L2 == 30) || (d.L1 == 24 && d.L2 == 24));
+}
+
+// sol_project for engines with one in-place FFT buffer (E::kStreamProj: the float-float engine),
+// without staging the three components: the Poisson pass reads them from the work fields and keeps
+// the potential d (natural rows, Dsv) beside the FFT buffer; after the pressure transform and the
+// harmonic coefficients the final pass reads the components again (L2: the same tile was read
+// moments before) and forms v - i k d - (harmonic correction) in the same order of operations as
+// vel_project.  Shared memory: X[L][TK] + Dsv[nz][TK] + per-warp wall sums (of vz and, for the
+// FP32 pressure transform, of d), which at a tile width of 8 fits where vel_project's three
+// staged components fit only 4.
+template <typename T, class E>
+__device__ void vel_project_streamed(const Geo &g, const typename E::Desc &fd, const FusedArgs &a, const ColTile &t,
+                                     C2<T> *X, C2<T> *Dsv, double2 *red, double2 *coef) {
+    using V = C2<T>;
+    const int nz = g.nz, nzp = g.nzp, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
+    const int tile = nz * TK;
+    const V *w0 = (const V *)a.work[0], *w1 = (const V *)a.work[1], *w2 = (const V *)a.work[2];
+    const int nwarps = blockDim.x >> 5;
+    double2 *redd = red + 2 * nwarps * TK;                // wall sums of d
+    V *prw_wall = (V *)(coef + 2 * TK);                  // [TK][2]: the two wall rows of IFFT(d)
+    LapCol<T> *lcol = (LapCol<T> *)(prw_wall + 2 * TK);
+    const bool p32 = pressure_fp32_ok(a.z32);
+    float2 *X32 = (float2 *)X;
+    // ---- Poisson: d -> X (or its FP32 rounding -> X32) and Dsv (natural), wall sums of
+    //      vz - i kz d (and of d)
+    {
+        const int c = threadIdx.x & (TK - 1), k0 = threadIdx.x >> lgTK, kstep = blockDim.x >> lgTK;
+        const int kxc = min(kx0 + c, g.nxh - 1);
+        const T kx_ = g.KX<T>(kxc), ky_ = g.KY<T>(ky);
+        WallSum<T> ws, wsd;
+        if (threadIdx.x < kstep * TK) {
+#pragma unroll 2
+            for (int k = k0; k < nz; k += kstep) {
+                const int idx = k * TK + c;
+                V A = mk<T>(0, 0), B = mk<T>(0, 0), Cc = mk<T>(0, 0);
+                if (c < nv) {
+                    const unsigned q = fidx<T>(g, k, ky, kx0 + c);
+                    A = w0[q];
+                    B = w1[q];
+                    Cc = w2[q];
+                }
+                const T kz_ = g.KZ<T>(k);
+                const T k2 = kx_ * kx_ + ky_ * ky_ + kz_ * kz_;
+                const V s = mk<T>(kx_ * A.x + ky_ * B.x + kz_ * Cc.x, kx_ * A.y + ky_ * B.y + kz_ * Cc.y);
+                const T ik2 = (T)1 / k2;
+                V D = mk<T>(s.y * ik2, -s.x * ik2);
+                if (k == 0 && ky == 0 && kx0 + c == 0) D = mk<T>(0, 0);
+                Cc = csub(Cc, cimk(kz_, D));
+                if (p32) {
+                    if constexpr (is_ff<T>) X32[idx] = make_float2(D.x.hi + D.x.lo, D.y.hi + D.y.lo);
+                    wsd.add(g, D, k);
+                } else {
+                    X[idx] = D;
+                }
+                Dsv[idx] = D;
+                ws.add(g, Cc, k);
+            }
+        }
+        ws.warp_reduce(TK);
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (lane < TK) ws.store(red + 2 * (warp * TK + lane));
+        if (p32) {
+            wsd.warp_reduce(TK);
+            if (lane < TK) wsd.store(redd + 2 * (warp * TK + lane));
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < TK) {
+        const int c = threadIdx.x;
+        WallSum<T> tot;
+        for (int q = 0; q < nwarps; q++) tot.load_add(red + 2 * (q * TK + c));
+        if constexpr (is_ff<T>) {
+            if (p32) {
+                WallSum<T> td;
+                for (int q = 0; q < nwarps; q++) td.load_add(redd + 2 * (q * TK + c));
+                prw_wall[2 * c] = td.q0;
+                prw_wall[2 * c + 1] = td.q1;
+            }
+        }
+        double2 b1 = tot.bottom(), b2 = tot.top();
+        const double inz = 1.0 / nz;
+        b1.x *= inz; b1.y *= inz; b2.x *= inz; b2.y *= inz;
+        const int kxc = min(kx0 + c, g.nxh - 1);
+        double2 c1, c2;
+        lap_coef_neumann(g, kxc, ky, b1, b2, c1, c2);
+        coef[2 * c] = c1;
+        coef[2 * c + 1] = c2;
+        LapCol<T> lc;
+        lc.kh = (T)g.lapc[((size_t)ky * g.nxh + kxc) * 3];
+        lc.c1 = mk<T>((T)c1.x, (T)c1.y);
+        lc.c2 = mk<T>((T)c2.x, (T)c2.y);
+        lc.k0 = kxc == 0 && ky == 0;
+        lcol[c] = lc;
+    }
+    __syncthreads();
+    // ---- pressure: pr = IFFT_z(d)/nz + a(z) on the physical rows
+    {
+        V *R = X;
+        if (p32) {
+            if (a.z32.L1 == 36) pressure_fp32<36, 30>(X32, TK, a.z32);
+            else pressure_fp32<24, 24>(X32, TK, a.z32);
+        } else {
+            R = E::run(X, nullptr, TK, fd, +1);
+        }
+        V *prw = (V *)a.pr;
+        const T inz = (T)1 / (T)nz, Lz = (T)g.Lz;
+        for (int idx = threadIdx.x; idx < nzp * TK; idx += blockDim.x) {
+            const int k = idx >> lgTK, c = idx & (TK - 1);
+            if (c >= nv) continue;
+            V pa, pb;
+            lap_profile_t<T>(lcol[c], g.ZZ<T>(k), Lz, pa, pb);
+            if constexpr (is_ff<T>) {
+                const LapCol<T> &p = lcol[c];
+                if ((k == 0 || k == nzp - 1) && !p.k0) {
+                    const ff e(g.lapc[((size_t)ky * g.nxh + min(kx0 + c, g.nxh - 1)) * 3 + 1]);
+                    pa = k == 0 ? mk<T>(p.c1.x * e + p.c2.x, p.c1.y * e + p.c2.y)
+                                : mk<T>(p.c1.x + p.c2.x * e, p.c1.y + p.c2.y * e);
+                }
+            }
+            V dv;
+            if (p32) {
+                if (k == 0 || k == nzp - 1) dv = prw_wall[2 * c + (k == 0 ? 0 : 1)];
+                else dv = from_f2<T>(X32[k * TK + c]);
+            } else {
+                dv = R[E::pos(k, fd) * TK + c];
+            }
+            prw[fidx<T>(g, k, ky, kx0 + c)] = mk<T>(dv.x * inz + pa.x, dv.y * inz + pa.y);
+        }
+        __syncthreads();
+    }
+    // ---- v - i k d, then the harmonic correction (as in vel_project), stored
+    {
+        const V *E1 = (const V *)a.hspec[0], *E2 = (const V *)a.hspec[1];
+        tile_load_async(X, E1 + t.col0, t.zs, nz, TK, nv);
+        tile_load_async(X + tile, E2 + t.col0, t.zs, nz, TK, nv);
+        async_wait();
+        __syncthreads();
+        V *o0 = (V *)a.vout[0], *o1 = (V *)a.vout[1], *o2 = (V *)a.vout[2];
+        const T ky_ = g.KY<T>(ky);
+        for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+            const int k = idx >> lgTK, c = idx & (TK - 1);
+            if (c >= nv) continue;
+            const int kx = kx0 + c;
+            const unsigned q = fidx<T>(g, k, ky, kx);
+            V A = w0[q], B = w1[q], Cc = w2[q];
+            const V D = Dsv[idx];
+            const T kx_ = g.KX<T>(kx), kz_ = g.KZ<T>(k);
+            A = csub(A, cimk(kx_, D));
+            B = csub(B, cimk(ky_, D));
+            Cc = csub(Cc, cimk(kz_, D));
+            const LapCol<T> lc = lcol[c];
+            const V e1 = X[idx], e2 = X[tile + idx];
+            V Ah, Bh;
+            if (lc.k0) {
+                Ah = mk<T>(lc.c1.x * e1.x + lc.c2.x * e2.x, lc.c1.x * e1.y + lc.c2.x * e2.y);
+                Bh = cscale(e2, lc.c1.x);
+            } else {
+                const V t1 = cmul(lc.c1, e1), t2 = cmul(lc.c2, e2);
+                Ah = cadd(t1, t2);
+                Bh = cscale(csub(t1, t2), lc.kh);
+            }
+            o0[q] = csub(A, cimk(kx_, Ah));
+            o1[q] = csub(B, cimk(ky_, Ah));
+            o2[q] = csub(Cc, Bh);
+        }
+    }
+}
+
 // One block per column tile for the whole velocity stage: smem = U[3][nz][TK] + FFT buffer(s)
 // + small FP64 scratch.  NL_{c+1} (or theta, for the buoyancy of c = z) is copied into the still
 // unused slot U[c+1] while component c is transformed.
@@ -580,6 +772,14 @@ __device__ __forceinline__ void fused_vproj_body(const Geo &g, const typename E:
     const int nz = g.nz;
     const ColTile t = col_tile<T>(g, TK, blockIdx);
     const int tile = nz * TK;
+    if constexpr (E::kStreamProj) {
+        V *X = (V *)smem_raw;
+        V *Dsv = X + (size_t)fd.L * TK;
+        double2 *red = (double2 *)(Dsv + tile);
+        double2 *coef = red + 4 * (blockDim.x >> 5) * TK;
+        vel_project_streamed<T, E>(g, fd, a, t, X, Dsv, red, coef);
+        return;
+    }
     V *U = (V *)smem_raw;
     V *X = U + 3 * tile;
     V *Y = X + (size_t)fd.L * TK;
@@ -591,7 +791,7 @@ __device__ __forceinline__ void fused_vproj_body(const Geo &g, const typename E:
     vel_project<T, E>(g, fd, a, t, U, X, Y, red, coef);
 }
 template <typename T, class E, int CTK = 0>
-__global__ void __launch_bounds__(E::kColThreads, is_ff<T> ? 1 : 2) k_fused_vproj(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
+__global__ void __launch_bounds__(E::kColThreads, is_ff<T> ? E::kMinBlocks : 2) k_fused_vproj(Geo g, typename E::Desc fd, FusedArgs a, int TKrt) {
     fused_vproj_body<T, E, CTK>(g, fd, a, TKrt, blockIdx);
 }
 

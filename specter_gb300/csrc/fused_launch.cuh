@@ -16,6 +16,10 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
     const size_t es = sizeof(C2<T>);
     const size_t L = (size_t)fd.L;
     auto smem = [&](int tk) -> size_t {
+        if (which == kFusedVProj && E::kStreamProj)  // vel_project_streamed: X, d, per-warp wall sums (two
+                                                     // sets), coefficients, the pressure's wall rows
+            return (E::kBuffers * L + (size_t)P.nz) * tk * es + (4 * ((size_t)E::kColThreads / 32) * tk + (size_t)tk * 2) * 16 +
+                   (size_t)tk * 2 * es + (size_t)tk * sizeof(LapCol<T>);
         if (which == kFusedVelocity || which == kFusedVProj) {
             const size_t thr = which == kFusedVelocity ? (size_t)E::wide_threads(tk) : (size_t)E::kColThreads;
             return (3 * (size_t)P.nz + E::kBuffers * L) * tk * es + (2 * thr + (size_t)tk * 2) * 16 +
@@ -32,7 +36,9 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
         // two blocks per SM
         // (float-float kernels run one block per SM anyway, their registers allow no more: they
         // may use most of the SM's shared memory)
-        const size_t budget = which == kFusedVelocity ? 200 * 1024 : is_ff<T> ? 220 * 1024 : 110 * 1024;
+        const size_t budget = which == kFusedVelocity ? 200 * 1024
+                              : is_ff<T>              ? (E::kMinBlocks > 1 ? 110 : 220) * 1024
+                                                      : 110 * 1024;
         for (int t : {16, 8, 4, 2, 1})
             if (t <= P.tile_cap[Plan::kTileFused] && smem(t) <= budget) { tk = t; break; }
         if (!tk) { set_error("z length too large for the fused column kernels"); return ERR_SHAPE; }

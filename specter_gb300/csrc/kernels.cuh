@@ -55,6 +55,7 @@ template <typename T, int NT = kThreads>
 struct GenericFFT {
     using Desc = FFTDesc;
     static constexpr int kBuffers = 2;
+    static constexpr bool kStreamProj = false;
     static constexpr int kMinBlocks = 1;
     static constexpr int kColThreads = NT;
     static constexpr int kWideThreads = NT;
@@ -76,6 +77,7 @@ template <typename T, int L1, int L2, bool OUTLINE = false>
 struct FourStep {
     using Desc = FFT4Desc;
     static constexpr int kBuffers = 1;
+    static constexpr bool kStreamProj = false;
     static constexpr int kMinBlocks = 2;  // cap registers at 128 so two blocks share an SM
     static constexpr int kColThreads = kThreads;
     // Kernels that run one block per SM (the fused velocity kernel) may take enough threads for

@@ -119,6 +119,11 @@ struct Plan {
     // float-float column kernels: 1 = the three-step Bluestein engine (ffblue.cuh) where the z
     // length has one, 0 = always the generic engine
     int ff_engine = 1;
+    // block shape of those kernels on the three-step engine: 0 = one 576-thread block per SM
+    // (tile width 8), 1 = two 288-thread blocks (width 4); for the projection and for the other
+    // column kernels separately
+    int ff_pair_proj = 0;
+    int ff_pair_cols = 0;
     int capped(int t, int kind) const { return t < tile_cap[kind] ? t : tile_cap[kind]; }
     long long launches = 0;
     bool profile = false;
