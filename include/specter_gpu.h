@@ -196,7 +196,9 @@ int specter_plan_tile_caps(specter_plan *plan, const int caps[4]);
  * "ff_engine" (1, the default: those kernels use the three-step register Bluestein engine when
  * nz + C lies in (270, 540]; 0: always the generic engine), "ff_pair_proj" and "ff_pair_cols"
  * (0/1: on that engine, the projection kernel and the other column kernels run as one 576-thread
- * block per SM or as two 288-thread blocks; the autotuner picks them) */
+ * block per SM or as two 288-thread blocks; the autotuner picks them), "ff_zoom" (1, the default:
+ * on that engine the wall round trips are window corrections of the spectrum when C + 2d = 35 and
+ * nz + C + 34 <= 576; 0: an inverse and a forward transform each) */
 int specter_plan_set_option(specter_plan *plan, const char *name, int value);
 /* the current value of a named plan option (the names above); no reference counterpart */
 int specter_plan_get_option(specter_plan *plan, const char *name, int *value);

@@ -671,6 +671,7 @@ int specter_plan_set_option(specter_plan *plan, const char *name, int value) {
     if (!strcmp(name, "ff_engine")) { P.ff_engine = value ? 1 : 0; return SPECTER_OK; }
     if (!strcmp(name, "ff_pair_proj")) { P.ff_pair_proj = value ? 1 : 0; return SPECTER_OK; }
     if (!strcmp(name, "ff_pair_cols")) { P.ff_pair_cols = value ? 1 : 0; return SPECTER_OK; }
+    if (!strcmp(name, "ff_zoom")) { P.ff_zoom = value ? 1 : 0; return SPECTER_OK; }
     if (!strcmp(name, "ff_threads")) {
         if (value != 256 && value != 384) { set_error("ff_threads is 256 or 384"); return SPECTER_ERR_ARG; }
         P.ff_threads = value;
@@ -693,7 +694,8 @@ int specter_plan_get_option(specter_plan *plan, const char *name, int *value) {
     const Plan &P = *plan->p;
     const struct { const char *n; int v; } opts[] = {
         {"velocity_split", P.velocity_split}, {"ff_threads", P.ff_threads}, {"ff_engine", P.ff_engine},
-        {"ff_pair_proj", P.ff_pair_proj},     {"ff_pair_cols", P.ff_pair_cols}, {"tile_cap_z", P.tile_cap[0]},
+        {"ff_pair_proj", P.ff_pair_proj},     {"ff_pair_cols", P.ff_pair_cols}, {"ff_zoom", P.ff_zoom},
+        {"tile_cap_z", P.tile_cap[0]},
         {"tile_cap_y", P.tile_cap[1]},        {"tile_cap_x", P.tile_cap[2]},   {"tile_cap_fused", P.tile_cap[3]}};
     for (const auto &o : opts)
         if (!strcmp(name, o.n)) { *value = o.v; return SPECTER_OK; }

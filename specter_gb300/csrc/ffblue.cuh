@@ -52,8 +52,10 @@ struct FFBTab {
 };
 
 struct FFBDesc {
-    int n, L, blue;
-    const ffc *tab;  // FFBTab::kLen entries (global memory, or shared once staged)
+    int n, L, blue;   // L: rows of the kernels' FFT buffer (>= the transform's 1080)
+    const ffc *tab;   // FFBTab::kLen entries (global memory, or shared once staged)
+    const ffc *ztab;  // wall round trips as window corrections (ffzoom.cuh), or null
+    int zj0;          // first window row (nzp - d)
 };
 
 namespace ffb {
@@ -338,30 +340,5 @@ __device__ __noinline__ void run_out(Q *X, const Q *tab, int n, int sign) {
 }
 
 }  // namespace ffb
-
-// Engine interface of the fused column kernels (kernels.cuh: GenericFFT, FourStep) for the
-// float-float kernels on this transform: one in-place buffer, natural order in and out, tables
-// through the read-only cache (measured as fast as staging them in shared memory), NT threads,
-// MINB blocks per SM.
-template <int NT, int MINB = 1>
-struct FFBlue {
-    using Desc = FFBDesc;
-    static constexpr int kBuffers = 1;
-    static constexpr bool kStreamProj = true;  // the projection without staged components
-    static constexpr int kMinBlocks = MINB;
-    static constexpr int kColThreads = NT;
-    static constexpr int kWideThreads = NT;
-    static int wide_threads(int) { return NT; }
-    static __device__ __forceinline__ ffc *run(ffc *X, ffc *, int B, const Desc &d, int sign) {
-        if (B == 8) ffb::run_out<8, NT>(X, d.tab, d.n, sign);
-        else if (B == 4) ffb::run_out<4, NT>(X, d.tab, d.n, sign);
-        else if (B == 2) ffb::run_out<2, NT>(X, d.tab, d.n, sign);
-        else ffb::run_out<1, NT>(X, d.tab, d.n, sign);
-        return X;
-    }
-    static __device__ __forceinline__ ffc *run_perm(ffc *X, ffc *Y, int B, const Desc &d, int sign) { return run(X, Y, B, d, sign); }
-    static __device__ __forceinline__ int pos(int k, const Desc &) { return k; }
-    static __device__ __forceinline__ int pos_stride(int D, const Desc &) { return D; }
-};
 
 }  // namespace sg

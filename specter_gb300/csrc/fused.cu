@@ -186,7 +186,7 @@ int fused_create(Plan &P, const StageParams &sp, FusedState **out) {
         }
         ok = ok && cudaMalloc(&fs->prq, P.field_bytes()) == cudaSuccess;
         if (ok) {
-            if (const int st2 = build_ffb_table(fs->ffb, P.nz)) {
+            if (const int st2 = build_ffb_table(fs->ffb, P.nz, P.nzp - P.oz, P.cz + 2 * P.oz)) {
                 fused_destroy(fs);
                 return st2;
             }
@@ -261,7 +261,14 @@ static int launch(Plan &P, const FusedState *fs, const FusedArgs &a, int which, 
     if constexpr (is_ff<T>) {
         // the three-step register engine where the z length has its tables (2.6x the generic
         // engine's transform rate at n = 538), else the generic Stockham engine
-        if (fs->ffb.ok && P.ff_engine) return ffb_fused(P, fs->ffb.d, a, which, bytes);
+        if (fs->ffb.ok && P.ff_engine) {
+            FFBDesc d = fs->ffb.d;
+            if (!P.ff_zoom) {  // plain round trips (two transforms each)
+                d.ztab = nullptr;
+                d.L = FFBTab::L;
+            }
+            return ffb_fused(P, d, a, which, bytes);
+        }
         if (P.ff_threads == 256) return launch_fused<ff, GenericFFT<ff, 256>>(P, fs->tzq.d, a, which, bytes);
         return launch_fused<ff, GenericFFT<ff, 384>>(P, fs->tzq.d, a, which, bytes);
     } else {

@@ -28,7 +28,7 @@ ffc to_ffc(const cld &v) {
 // w_1080^(n3 j), the inverse transform's chirp exp(+i pi k^2 / n), and the filter: the length-L
 // DFT of exp(-i pi m^2 / n), m = -(n-1) .. n-1 (wrapped), times 1/L, at frequency
 // f = k1 + 8 k2 + 120 k3 stored in slot (k1 * 15 + k2) * 9 + k3 (the order step C reads).
-int build_ffb_table(FFBTable &t, int n) {
+int build_ffb_table(FFBTable &t, int n, int j0, int win) {
     using T = FFBTab;
     t = FFBTable{};
     if (n > T::kMaxN || 4 * n <= T::L) return OK;
@@ -75,11 +75,74 @@ int build_ffb_table(FFBTable &t, int n) {
     t.d.blue = 1;
     t.d.tab = (const ffc *)t.mem;
     t.ok = 1;
+    // the wall round trips as window corrections: C + 2d = 35 window rows and n + 34 <= 576
+    if (win == FFZTab::kWin) {
+        const std::vector<ffc> z = ffz_table_host(n, j0);
+        if (!z.empty()) {
+            if (cudaMalloc(&t.zmem, z.size() * sizeof(ffc)) != cudaSuccess) {
+                cudaGetLastError();
+                free_ffb_table(t);
+                set_error("cudaMalloc failed (float-float window tables)");
+                return ERR_OOM;
+            }
+            if (cudaMemcpy(t.zmem, z.data(), z.size() * sizeof(ffc), cudaMemcpyHostToDevice) != cudaSuccess) {
+                free_ffb_table(t);
+                return check_launch("float-float window tables");
+            }
+            t.d.ztab = (const ffc *)t.zmem;
+            t.d.zj0 = j0;
+            // the kernels' FFT buffer also holds the window scratch after the spectrum
+            const int rows = n + FFZTab::L + 2 * FFZTab::kWin;
+            if (rows > t.d.L) t.d.L = rows;
+        }
+    }
     return OK;
+}
+
+// The window-correction table (ffzoom.cuh) for z length n and window start j0, in long double.
+// Chirp c_k = exp(+i pi k^2 / n); filters G = FFT_L(g) / L with g[s] = conj(c_{j0+s}),
+// s = -(n-1) .. kWin-1, and H = FFT_L(h) / L with h[s] = c_{s-j0}, s = -(kWin-1) .. n-1, both
+// stored at s mod L (disjoint for n + kWin - 1 <= L), at frequency f = k1 + 8 k2 + 64 k3 in slot
+// (k1 * 8 + k2) * 9 + k3.  Empty when n is odd or too long.
+namespace {
+cld chirp_l(long k, long n) {  // exp(+i pi k^2 / n), period n for even n
+    k = ((k % n) + n) % n;
+    const long double a = kPi * (long double)((k * k) % (2L * n)) / (long double)n;
+    return cld(cosl(a), sinl(a));
+}
+}  // namespace
+
+std::vector<ffc> ffz_table_host(int n, int j0) {
+    using T = FFZTab;
+    if (n % 2 || n > T::kMaxN || j0 < 0 || j0 >= n) return {};
+    std::vector<ffc> h(T::kLen);
+    for (auto &e : h) e.x = e.y = ff(0.f, 0.f);
+    for (int n2 = 0; n2 < T::L2; n2++)
+        for (int k1 = 0; k1 < T::L1; k1++) h[T::kOffTw1 + n2 * T::kTw1S + k1] = to_ffc(root_l((long)n2 * k1, T::J));
+    for (int n3 = 0; n3 < T::L3; n3++)
+        for (int j = 0; j < T::J; j++) h[T::kOffTw2 + n3 * T::kTw2S + j] = to_ffc(root_l((long)n3 * j, T::L));
+    for (int k = 0; k < n; k++) h[T::kOffChirp + k] = to_ffc(chirp_l(k, n));
+    std::vector<cld> g(T::L, cld(0)), hh(T::L, cld(0)), w(T::L);
+    for (int s = -(n - 1); s <= T::kWin - 1; s++) g[(s + T::L) % T::L] = std::conj(chirp_l(j0 + s, n));
+    for (int s = -(T::kWin - 1); s <= n - 1; s++) hh[(s + T::L) % T::L] = chirp_l(s - j0, n);
+    for (int k = 0; k < T::L; k++) w[k] = root_l(k, T::L);
+    for (int f = 0; f < T::L; f++) {
+        cld sg(0), sh(0);
+        for (int m = 0; m < T::L; m++) {
+            const cld r = w[((long)f * m) % T::L];
+            sg += g[m] * r;
+            sh += hh[m] * r;
+        }
+        const int k1 = f % T::L1, k2 = (f / T::L1) % T::L2, k3 = f / T::J;
+        h[T::kOffG + (k1 * T::L2 + k2) * T::L3 + k3] = to_ffc(sg / (long double)T::L);
+        h[T::kOffH + (k1 * T::L2 + k2) * T::L3 + k3] = to_ffc(sh / (long double)T::L);
+    }
+    return h;
 }
 
 void free_ffb_table(FFBTable &t) {
     if (t.mem) cudaFree(t.mem);
+    if (t.zmem) cudaFree(t.zmem);
     t = FFBTable{};
 }
 

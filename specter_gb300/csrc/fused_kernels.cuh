@@ -235,6 +235,53 @@ __device__ __forceinline__ C2<T> *nl_forward(const Geo &g, const typename E::Des
     return E::run(X, Y, TK, fd, -1);
 }
 
+// A wall round trip of the float-float kernels as a window correction (ffzoom.cuh): X holds the
+// spectrum (rows [0, nz), natural); window row p is physical row (nzp - d + p) mod nz: p < d the
+// top wall-adjacent rows (p = d - 1 the top wall), d <= p < d + C the continuation rows, the rest
+// the bottom rows (p = d + C the bottom wall).  The window values of the inverse transform are
+// scaled by 1/nz (goto_domain), the wall rows take wall(top, col) when `walls`, the continuation
+// rows are rebuilt from the 2d wall-adjacent rows with the float-float sums of fc_continuation,
+// and the forward transform of (new - old) is added to X.  X is the updated spectrum, visible to
+// all threads, on return.  Scratch: rows [nz, nz + 576 + 2 kWin) of X (the engine's Desc.L).
+template <typename T, class E, class Wall>
+__device__ __forceinline__ void zoom_round_trip(const Geo &g, const typename E::Desc &fd, C2<T> *X, int TK, bool walls,
+                                                Wall wall) {
+    using V = C2<T>;
+    const int nz = g.nz, d = g.oz, C = g.cz, lgTK = lg2(TK);
+    V *W = X + (size_t)nz * TK, *Wv = W + (size_t)FFZTab::L * TK, *Dv = Wv + (size_t)FFZTab::kWin * TK;
+    E::window(X, W, Wv, fd, TK);
+    const T inz = (T)1 / (T)nz;
+    for (int idx = threadIdx.x; idx < FFZTab::kWin * TK; idx += blockDim.x) {
+        const int p = idx >> lgTK, c = idx & (TK - 1);
+        const V u = cscale(Wv[idx], inz);
+        if (walls && (p == d - 1 || p == d + C)) {
+            const V w = wall(p == d - 1, c);
+            Dv[idx] = csub(w, u);
+            Wv[idx] = w;
+        } else {
+            Dv[idx] = mk<T>(0, 0);
+            Wv[idx] = u;
+        }
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < C * TK; idx += blockDim.x) {
+        const int ii = idx >> lgTK, c = idx & (TK - 1);
+        T ar = (T)0, ai = (T)0;
+        for (int jj = 0; jj < d; jj++) {
+            const V t = Wv[jj * TK + c], b = Wv[(C + 2 * d - 1 - jj) * TK + c];
+            const float2 q0 = __ldg((const float2 *)(g.dirq + ii + C * jj));
+            const float2 q1 = __ldg((const float2 *)(g.dirq + (C - 1 - ii) + C * jj));
+            const T w0 = T(q0.x, q0.y), w1 = T(q1.x, q1.y);
+            ar = ar + w0 * t.x + w1 * b.x;
+            ai = ai + w0 * t.y + w1 * b.y;
+        }
+        const int p = d + ii;
+        Dv[p * TK + c] = csub(mk<T>(ar, ai), Wv[p * TK + c]);
+    }
+    __syncthreads();
+    E::window_add(X, W, Dv, fd, TK);
+}
+
 // ----------------------------------------------------------------------------------------------
 // velocity: device functions shared by the one-block-per-tile kernel (k_fused_velocity) and the
 // split pair (k_fused_vcomp per component, k_fused_vproj for the projection)
@@ -335,6 +382,33 @@ __device__ void vel_walls(const Geo &g, const typename E::Desc &fd, const FusedA
     const int nz = g.nz, nzp = g.nzp, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
     const V *pr = (const V *)a.pr;
     const T wall_tmp = pick<T>(a.wall_tmp, a.f_wall_tmp, a.q_wall_tmp), inz = (T)1 / (T)nz;
+    if constexpr (E::kZoom) {
+        if (fd.ztab) {
+            if (!in_x) {
+                for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) X[idx] = Uc[idx];
+                __syncthreads();
+            }
+            // no-slip wall rows from the previous stage's pressure (noslip_z), as below
+            auto wall = [&](bool top, int c) -> V {
+                if (c >= nv) return mk<T>(0, 0);
+                const int kx = kx0 + c, k = top ? nzp - 1 : 0;
+                if (kx == 0 && ky == 0) return mk<T>((T)((double)g.nx * g.ny * a.vb[(top ? 2 : 0) + c3]), (T)0);
+                const V p = pr[fidx<T>(g, k, ky, kx)];
+                return cscale(cimk(c3 == 0 ? g.KX<T>(kx) : g.KY<T>(ky), p), wall_tmp);
+            };
+            zoom_round_trip<T, E>(g, fd, X, TK, true, wall);
+            for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+                const int k = idx >> lgTK, c = idx & (TK - 1);
+                if (wout) {
+                    if (c < nv) wout[fidx<T>(g, k, ky, kx0 + c)] = X[idx];
+                } else {
+                    Uc[idx] = X[idx];
+                }
+            }
+            if (!wout) __syncthreads();
+            return;
+        }
+    }
     if (!in_x) {
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) X[idx] = Uc[idx];
         __syncthreads();
@@ -694,7 +768,7 @@ template <typename T, class E>
 __global__ void __launch_bounds__(E::kWideThreads, 1) k_fused_velocity(Geo g, typename E::Desc fd, FusedArgs a, int TK) {
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int nz = g.nz, nzp = g.nzp, L = fd.L;
+    const int nz = g.nz, L = fd.L;
     const ColTile t = col_tile<T>(g, TK, blockIdx);
     const int tile = nz * TK;
     V *U = (V *)smem_raw;                       // 3 components, natural rows
@@ -731,7 +805,7 @@ __device__ __forceinline__ void fused_vcomp_body(const Geo &g, const typename E:
     const int TK = CTK ? CTK : TKrt;  // CTK: the tile width fixed at compile time, else 0
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int nz = g.nz, nzp = g.nzp;
+    const int nz = g.nz;
     const ColTile t = col_tile<T>(g, TK, blockIdx);
     const int c3 = blockIdx.z;
     V *Uc = (V *)smem_raw;
@@ -774,7 +848,7 @@ __device__ __forceinline__ void fused_vproj_body(const Geo &g, const typename E:
     const int tile = nz * TK;
     if constexpr (E::kStreamProj) {
         V *X = (V *)smem_raw;
-        V *Dsv = X + (size_t)fd.L * TK;
+        V *Dsv = X + (size_t)E::kProjRows * TK;
         double2 *red = (double2 *)(Dsv + tile);
         double2 *coef = red + 4 * (blockDim.x >> 5) * TK;
         vel_project_streamed<T, E>(g, fd, a, t, X, Dsv, red, coef);
@@ -860,8 +934,34 @@ __global__ void __launch_bounds__(E::kColThreads, E::kMinBlocks) k_fused_theta(G
     }
     // 2. s_imposebc (IFFT, 1/nz, walls = 0, continuation + FFT), then fc_filter.  With one
     //    in-place buffer in natural order (the Bluestein four-step engine) every step finishes
-    //    in X; otherwise through Th.
-    {
+    //    in X; otherwise through Th.  Float-float kernels with window tables: as a window
+    //    correction of the spectrum (zoom_round_trip).
+    bool zoomed = false;
+    if constexpr (E::kZoom) {
+        if (fd.ztab) {
+            zoom_round_trip<T, E>(g, fd, X, TK, true, [&](bool, int) { return mk<T>(0, 0); });
+            if (a.rot) {
+                V *out = (V *)a.vout[3];
+                for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+                    const int k = idx >> lgTK, c = idx & (TK - 1);
+                    if (c < nv) out[colq(k, c)] = X[idx];
+                }
+                return;
+            }
+            for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+                const int k = idx >> lgTK, c = idx & (TK - 1);
+                const int kx = min(kx0 + c, g.nxh - 1);
+                V v = X[idx];
+                v = cscale(v, g.FX<T>(kx));
+                v = cscale(v, g.FY<T>(ky));
+                v = cscale(v, g.FZ<T>(k));
+                X[idx] = v;
+            }
+            __syncthreads();
+            zoomed = true;
+        }
+    }
+    if (!zoomed) {
         V *R = E::run(X, Y, TK, fd, +1);
         bool inplace = R == X && fd.blue;
         V *P = inplace ? X : Th;
@@ -902,7 +1002,20 @@ __global__ void __launch_bounds__(E::kColThreads, E::kMinBlocks) k_fused_theta(G
             __syncthreads();
         }
     }
-    // 3. c2r -> /(nx ny nz) -> r2c: z-inverse and 1/nz here; kx = 0 and nx/2 go to the side buffer
+    // 3. c2r -> /(nx ny nz) -> r2c: z-inverse and 1/nz here; kx = 0 and nx/2 go to the side buffer.
+    //    Tiles without those two columns, with window tables: continuation rows rebuilt as a
+    //    window correction (no wall rows change).
+    if constexpr (E::kZoom) {
+        if (fd.ztab && kx0 > 0 && kx0 + TK < g.nxh) {
+            zoom_round_trip<T, E>(g, fd, X, TK, false, [&](bool, int) { return mk<T>(0, 0); });
+            V *out = (V *)a.vout[3];
+            for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+                const int k = idx >> lgTK, c = idx & (TK - 1);
+                if (c < nv) out[colq(k, c)] = X[idx];
+            }
+            return;
+        }
+    }
     {
         V *R = E::run(X, Y, TK, fd, +1);
         const bool inplace = R == X && fd.blue;

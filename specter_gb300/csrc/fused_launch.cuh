@@ -3,7 +3,7 @@
 
 #include <string>
 
-#include "ffblue.cuh"
+#include "ffzoom.cuh"
 #include "fused_kernels.cuh"
 
 namespace sg {
@@ -18,7 +18,7 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
     auto smem = [&](int tk) -> size_t {
         if (which == kFusedVProj && E::kStreamProj)  // vel_project_streamed: X, d, per-warp wall sums (two
                                                      // sets), coefficients, the pressure's wall rows
-            return (E::kBuffers * L + (size_t)P.nz) * tk * es + (4 * ((size_t)E::kColThreads / 32) * tk + (size_t)tk * 2) * 16 +
+            return ((size_t)E::kProjRows + (size_t)P.nz) * tk * es + (4 * ((size_t)E::kColThreads / 32) * tk + (size_t)tk * 2) * 16 +
                    (size_t)tk * 2 * es + (size_t)tk * sizeof(LapCol<T>);
         if (which == kFusedVelocity || which == kFusedVProj) {
             const size_t thr = which == kFusedVelocity ? (size_t)E::wide_threads(tk) : (size_t)E::kColThreads;
@@ -98,9 +98,11 @@ int fast_fused(Plan &P, const FusedArgs &a, int which, double bytes);
 struct FFBTable {
     FFBDesc d{};
     void *mem = nullptr;
+    void *zmem = nullptr;  // window-correction tables (ffzoom.cuh), when the window fits
     int ok = 0;
 };
-int build_ffb_table(FFBTable &t, int n);
+// n = nz + C; window: first row j0 = nzp - d and win = C + 2d rows
+int build_ffb_table(FFBTable &t, int n, int j0, int win);
 void free_ffb_table(FFBTable &t);
 // the float-float column kernels on that engine (fused_ffb.cu)
 int ffb_fused(Plan &P, const FFBDesc &d, const FusedArgs &a, int which, double bytes);

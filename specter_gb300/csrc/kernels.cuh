@@ -56,6 +56,8 @@ struct GenericFFT {
     using Desc = FFTDesc;
     static constexpr int kBuffers = 2;
     static constexpr bool kStreamProj = false;
+    static constexpr int kProjRows = 0;
+    static constexpr bool kZoom = false;
     static constexpr int kMinBlocks = 1;
     static constexpr int kColThreads = NT;
     static constexpr int kWideThreads = NT;
@@ -78,6 +80,8 @@ struct FourStep {
     using Desc = FFT4Desc;
     static constexpr int kBuffers = 1;
     static constexpr bool kStreamProj = false;
+    static constexpr int kProjRows = 0;
+    static constexpr bool kZoom = false;
     static constexpr int kMinBlocks = 2;  // cap registers at 128 so two blocks share an SM
     static constexpr int kColThreads = kThreads;
     // Kernels that run one block per SM (the fused velocity kernel) may take enough threads for

@@ -124,6 +124,9 @@ struct Plan {
     // column kernels separately
     int ff_pair_proj = 0;
     int ff_pair_cols = 0;
+    // on that engine, wall round trips as window corrections of the spectrum (1) or as an inverse
+    // and a forward transform (0)
+    int ff_zoom = 1;
     int capped(int t, int kind) const { return t < tile_cap[kind] ? t : tile_cap[kind]; }
     long long launches = 0;
     bool profile = false;
