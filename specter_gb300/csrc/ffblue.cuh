@@ -288,15 +288,21 @@ __device__ __forceinline__ void bluestein(Q *X, const Q *tab, int n, int sign) {
         Q d[9];
 #pragma unroll
         for (int n3 = 0; n3 < 9; n3++) d[n3] = X[(base + n3) * TK + c];
-        dft9<-1>(d);
+        // DFT_9, filter, inverse DFT_9 with one DFT_9 body (the inverse is conj(DFT_9(conj x))):
+        // half the instruction footprint of the step
         const Q *fl = filt + j * T::L3;
+#pragma unroll 1
+        for (int pass = 0; pass < 2; pass++) {
+            dft9<-1>(d);
+            if (pass == 0) {
 #pragma unroll
-        for (int k3 = 0; k3 < 9; k3++) d[k3] = qmul(d[k3], tab_ld<TS>(fl + k3));
-        dft9<+1>(d);
+                for (int k3 = 0; k3 < 9; k3++) d[k3] = qconj(qmul(d[k3], tab_ld<TS>(fl + k3)));
+            }
+        }
         const Q *tw = tw2 + k1 + T::L1 * k2;
-        X[base * TK + c] = d[0];
+        X[base * TK + c] = qconj(d[0]);
 #pragma unroll
-        for (int m3 = 1; m3 < 9; m3++) X[(base + m3) * TK + c] = qmulc(d[m3], tab_ld<TS>(tw + m3 * T::kTw2S));
+        for (int m3 = 1; m3 < 9; m3++) X[(base + m3) * TK + c] = qconj(qmul(d[m3], tab_ld<TS>(tw + m3 * T::kTw2S)));
     }
     __syncthreads();
     // step B': inverse DFT_15 over k2, w_120^(-m2 k1)

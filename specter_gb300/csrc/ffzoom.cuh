@@ -89,15 +89,23 @@ __device__ __forceinline__ void steps_bcc(Q *W, const Q *tab, const Q *filt) {
         Q d[9];
 #pragma unroll
         for (int n3 = 0; n3 < 9; n3++) d[n3] = W[(base + n3) * TK + c];
-        dft9<-1>(d);
+        // DFT_9, filter, inverse DFT_9 with one DFT_9 body (half the instruction footprint of
+        // this, the largest step): the inverse is conj(DFT_9(conj x)), so the first pass leaves
+        // the conjugated filtered values and the second pass's result is the conjugated inverse
         const Q *fl = filt + j * T::L3;
+#pragma unroll 1
+        for (int pass = 0; pass < 2; pass++) {
+            dft9<-1>(d);
+            if (pass == 0) {
 #pragma unroll
-        for (int k3 = 0; k3 < 9; k3++) d[k3] = qmul(d[k3], ldq(fl + k3));
-        dft9<+1>(d);
+                for (int k3 = 0; k3 < 9; k3++) d[k3] = qconj(qmul(d[k3], ldq(fl + k3)));
+            }
+        }
+        // inverse output conj(d) times conj(w): conj(d w)
         const Q *tw = tw2 + k1 + T::L1 * k2;
-        W[base * TK + c] = d[0];
+        W[base * TK + c] = qconj(d[0]);
 #pragma unroll
-        for (int m3 = 1; m3 < 9; m3++) W[(base + m3) * TK + c] = qmulc(d[m3], ldq(tw + m3 * T::kTw2S));
+        for (int m3 = 1; m3 < 9; m3++) W[(base + m3) * TK + c] = qconj(qmul(d[m3], ldq(tw + m3 * T::kTw2S)));
     }
     __syncthreads();
 }
