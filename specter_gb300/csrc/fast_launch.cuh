@@ -131,17 +131,20 @@ int xnl(Plan &P, const XNLArgs &a, double bytes) {
     for (int t : {16, 8, 4, 2, 1})
         if (t <= P.tile_cap[Plan::kTileX] && x_nl_elems<E>(P.tx4.d, P.nxh, P.H, t) * sizeof(float2) <= kMaxSmem) { rb = t; break; }
     if (!rb) return kNoFast;
-    const size_t sm = x_nl_elems<E>(P.tx4.d, P.nxh, P.H, rb) * sizeof(float2);
-    // the production x lengths (H = 256, 128) at 8 rows run a copy with the row count fixed
+    // the production x lengths (H = 256, 128) at 8 rows run a copy with the row count fixed,
+    // which takes the pipelined form (two FFT buffers, row-major staging: x_nl_pipe_elems)
     constexpr bool kFixed = L1 == 16 && (L2 == 16 || L2 == 8);
-    if (P.batch) {  // record for a batched launch (batch.h)
+    const bool fixed = kFixed && rb == 8;
+    if (P.batch) {  // record for a batched launch (batch.h): the plain body
+        const size_t smb = x_nl_elems<E>(P.tx4.d, P.nxh, P.H, rb) * sizeof(float2);
         using R = PassRec<E, XNLArgs>;
         const R r{{0, cdiv(a.nrows * P.ny, rb), 1, 1}, P.geo, P.tx4.d, a.prepared(), rb};
         batch_add(*P.batch, r, (const void *)k_x_nonlinear_batch<float, E>,
-                  &batch_launch<R, k_x_nonlinear_batch<float, E>, kThreads>, sm, "x_nonlinear", bytes);
+                  &batch_launch<R, k_x_nonlinear_batch<float, E>, kThreads>, smb, "x_nonlinear", bytes);
         return OK;
     }
-    auto k = (kFixed && rb == 8) ? k_x_nonlinear<float, E, kFixed ? 8 : 0> : k_x_nonlinear<float, E>;
+    const size_t sm = (fixed ? x_nl_pipe_elems(P.nxh, P.H, rb) : x_nl_elems<E>(P.tx4.d, P.nxh, P.H, rb)) * sizeof(float2);
+    auto k = fixed ? k_x_nonlinear<float, E, kFixed ? 8 : 0> : k_x_nonlinear<float, E>;
     smem_attr(k, sm);
     Scope s(P, "x_nonlinear", bytes);
     k<<<dim3(cdiv(a.nrows * P.ny, rb)), kThreads, sm, P.stream>>>(P.geo, P.tx4.d, a.prepared(), rb);

@@ -218,8 +218,10 @@ __device__ __forceinline__ C2<T> gtw(const C2<T> *tw, int t) {
 constexpr int ct_lg2(int b) { return b <= 1 ? 0 : 1 + ct_lg2(b / 2); }
 
 // ---- natural -> permuted (steps A, B) ---------------------------------------------------------
-// PFA: prime-factor register DFTs (dft_pfa) instead of the mixed-radix chain (dft_reg)
-template <typename T, int L1, int L2, int SIGN, bool PFA = true>
+// PFA: prime-factor register DFTs (dft_pfa) instead of the mixed-radix chain (dft_reg).
+// WAIT: complete the calling thread's asynchronous copies before the final barrier, so that
+// copies issued before the transform are visible to the whole block when it returns.
+template <typename T, int L1, int L2, int SIGN, bool PFA = true, bool WAIT = false>
 __device__ __forceinline__ void fft4_np_impl(C2<T> *X, int B, const FFT4Desc &d) {
     const int lgB = lg2(B);
     constexpr int L = L1 * L2;
@@ -245,6 +247,7 @@ __device__ __forceinline__ void fft4_np_impl(C2<T> *X, int B, const FFT4Desc &d)
 #pragma unroll
         for (int k2 = 0; k2 < L2; k2++) X[(L2 * k1 + k2) * B + c] = b[k2];
     }
+    if constexpr (WAIT) async_wait();
     __syncthreads();
     (void)L;
 }

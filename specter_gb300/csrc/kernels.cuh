@@ -117,6 +117,19 @@ struct FourStep {
         else fft4_pn<T, L1, L2, +1>(X, B, d);
         return X;
     }
+    // run(+1 or -1) that also completes the calling thread's asynchronous copies before its final
+    // barrier (copies issued before the call are visible to the block on return)
+    static __device__ __forceinline__ C2<T> *run_wait(C2<T> *X, C2<T> *Y, int B, const Desc &d, int sign) {
+        if (d.blue) {
+            C2<T> *R = run(X, Y, B, d, sign);
+            async_wait();
+            __syncthreads();
+            return R;
+        }
+        if (sign < 0) fft4_np_impl<T, L1, L2, -1, true, true>(X, B, d);
+        else fft4_np_impl<T, L1, L2, +1, true, true>(X, B, d);
+        return X;
+    }
     static __device__ __forceinline__ int pos(int k, const Desc &d) { return d.blue ? k : perm_pos<L1, L2>(k); }
     // pos(m + D) - pos(m) for every m, or -1 when that is not a constant
     static __device__ __forceinline__ int pos_stride(int D, const Desc &d) {
@@ -542,6 +555,189 @@ __device__ __forceinline__ const C2<T> *xnl_input(const XNLArgs &a, int t, int &
     return (const C2<T> *)(term == 0 ? a.u[i] : term == 1 ? a.dy[i] : a.dz[i]);
 }
 
+// ---- pipelined form (four-step engine, FP32, fixed row count) --------------------------------
+// Two FFT buffers: the pre-processing of input t+1 runs in the same phase as the products of
+// input t, and the copy of input t+2 into the staging buffer is completed inside the transform
+// of input t+1 (FourStep::run_wait), so each input costs one barrier besides the transform's
+// two.  The staging buffer is row-major, S[r * SK + k] (16-byte copies of (k, k+1) pairs; with
+// SK = 4 mod 16 the column reads of the pre-processing fall two to a bank), and
+// the forward R2C post-processing writes a row-major copy into the accumulator, free by then.
+__host__ __device__ inline int x_stage_stride(int nxh) { return ((nxh - 4 + 15) / 16) * 16 + 4; }
+
+__host__ __device__ inline size_t x_nl_pipe_elems(int nxh, int H, int RB) {
+    const size_t sk = (size_t)RB * x_stage_stride(nxh);
+    return (size_t)2 * H * RB + sk + (size_t)3 * H * RB + (sk > (size_t)H * RB ? sk : (size_t)H * RB);
+}
+
+// rows r < nv of a complex field (row stride ld) -> S[r * SK + k], k < nxh; rows nv <= r < RB are zero
+template <typename V>
+__device__ __forceinline__ void rows_load_rm(V *S, const V *src, unsigned ld, int nxh, int RB, int nv, int SK) {
+    static_assert(sizeof(V) == 8, "16-byte pair copies of single-precision complex values");
+    const int PP = (nxh + 1) >> 1;  // (k, k+1) pairs per row
+    const int sr = blockDim.x / PP, sp = blockDim.x - sr * PP;
+    int r = threadIdx.x / PP, p = threadIdx.x - r * PP;
+    for (int idx = threadIdx.x; idx < RB * PP; idx += blockDim.x) {
+        const int k = 2 * p;
+        V *d = S + r * SK + k;
+        if (r < nv) {
+            const V *gsrc = src + ((unsigned)r * ld + (unsigned)k);
+            if (k + 1 < nxh) cp_async<16>(d, gsrc);
+            else cp_async<8>(d, gsrc);
+        } else {
+            V z;
+            z.x = 0;
+            z.y = 0;
+            d[0] = z;
+            if (k + 1 < nxh) d[1] = z;
+        }
+        r += sr;
+        p += sp;
+        if (p >= PP) { p -= PP; r++; }
+    }
+    async_commit();
+}
+
+// c2r_pre from the row-major staging (same arithmetic)
+template <typename T>
+__device__ __forceinline__ void c2r_pre_rm(const Geo &g, const C2<T> *S, int SK, C2<T> *Z, int RB, int lgRB, int dx) {
+    using V = C2<T>;
+    const V *xtw = (const V *)g.xtw;
+    const int H = g.H, Hh = H >> 1;
+    for (int idx = threadIdx.x; idx < (Hh + 1) * RB; idx += blockDim.x) {
+        const int k = idx >> lgRB, r = idx & (RB - 1);
+        V xk = S[r * SK + k], xm = S[r * SK + H - k];
+        if (dx) {
+            xk = cimk(g.KX<T>(k), xk);
+            xm = cimk(g.KX<T>(H - k), xm);
+        }
+        if (k == 0) { xk.y = 0; xm.y = 0; }
+        const V xmc = cconj(xm);
+        const V e = cadd(xk, xmc);
+        V w = __ldg(xtw + k);
+        w.y = -w.y;  // exp(+2 pi i k / nx)
+        const V o = cmul(csub(xk, xmc), w);
+        Z[idx] = mk<T>(e.x - o.y, e.y + o.x);
+        if (k != 0 && 2 * k != H) Z[(H - k) * RB + r] = mk<T>(e.x + o.y, o.x - e.y);
+    }
+}
+
+// r2c_post into a row-major buffer: Z (output k of the forward transform from permuted input,
+// E::run_perm, which leaves natural order: row k) -> O[r * SK + k], k <= H
+template <typename T, class E>
+__device__ __forceinline__ void r2c_post_rm(const Geo &g, const typename E::Desc &fd, const C2<T> *Z, C2<T> *O, int SK,
+                                            int RB, int lgRB) {
+    using V = C2<T>;
+    const V *xtw = (const V *)g.xtw;
+    const int H = g.H, Hh = H >> 1;
+    (void)fd;
+    for (int idx = threadIdx.x; idx < (Hh + 1) * RB; idx += blockDim.x) {
+        const int k = idx >> lgRB, r = idx & (RB - 1);
+        const V zk = Z[k * RB + r], zm = cconj(Z[(k ? H - k : 0) * RB + r]);
+        const V e = cadd(zk, zm), d = csub(zk, zm);
+        const V t = cmul(d, __ldg(xtw + k));
+        O[r * SK + k] = mk<T>((T)0.5 * (e.x + t.y), (T)0.5 * (e.y - t.x));
+        if (2 * k != H) O[r * SK + H - k] = mk<T>((T)0.5 * (e.x - t.y), (T)-0.5 * (e.y + t.x));
+    }
+}
+
+// rows r < nv of O[r * SK + k] -> out[r * ld + k], k < nxh, 16-byte stores of (k, k+1) pairs
+template <typename V>
+__device__ __forceinline__ void rows_store_rm(V *out, unsigned ld, const V *O, int SK, int nxh, int nv) {
+    static_assert(sizeof(V) == 8, "16-byte pair stores of single-precision complex values");
+    const int PP = (nxh + 1) >> 1;
+    const int sr = blockDim.x / PP, sp = blockDim.x - sr * PP;
+    int r = threadIdx.x / PP, p = threadIdx.x - r * PP;
+    for (int idx = threadIdx.x; idx < nv * PP; idx += blockDim.x) {
+        const int k = 2 * p;
+        V *d = out + ((unsigned)r * ld + (unsigned)k);
+        const V *o = O + r * SK + k;
+        if (k + 1 < nxh) {
+            const float4 v = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+            *(float4 *)d = v;
+        } else {
+            d[0] = o[0];
+        }
+        r += sr;
+        p += sp;
+        if (p >= PP) { p -= PP; r++; }
+    }
+}
+
+template <typename T, class E, int RB>
+__device__ __forceinline__ void x_nonlinear_pipe(const Geo &g, const typename E::Desc &fd, const XNLArgs &a) {
+    constexpr int lgRB = RB == 16 ? 4 : RB == 8 ? 3 : RB == 4 ? 2 : RB == 2 ? 1 : 0;
+    using V = C2<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int H = g.H, nxh = g.nxh, SK = x_stage_stride(nxh);
+    V *Xb[2];
+    Xb[0] = (V *)smem_raw;                 // two FFT buffers of H x RB
+    Xb[1] = Xb[0] + (size_t)H * RB;
+    V *S = Xb[1] + (size_t)H * RB;         // RB x SK row-major staging
+    V *U = S + (size_t)RB * SK;            // 3 x H x RB physical velocity rows
+    V *A = U + (size_t)3 * H * RB;         // H x RB accumulator; RB x SK output staging after term 2
+    const int nc = a.c1 - a.c0, T_in = 3 + 3 * nc;
+    const int row0 = blockIdx.x * RB, nv = min(RB, a.nrows * g.ny - row0);
+    const T tmp = pick<T>(a.tmp, a.tmp_f);
+    const size_t off = (size_t)row0 * g.ldx;
+    const unsigned ld = (unsigned)g.ldx;
+    int term, i, tn, in_;
+    // input 0 into Xb[0]; input 1 copied into S during the first transform
+    rows_load_rm(S, xnl_input<T>(a, 0, term, i) + off, ld, nxh, RB, nv, SK);
+    async_wait();
+    __syncthreads();
+    c2r_pre_rm<T>(g, S, SK, Xb[0], RB, lgRB, term == 0);
+    __syncthreads();
+    if (T_in > 1) rows_load_rm(S, xnl_input<T>(a, 1, tn, in_) + off, ld, nxh, RB, nv, SK);
+    E::run_wait(Xb[0], nullptr, RB, fd, +1);
+    // output m of a transform sits at row E::pos(m); m advances by D per iteration, so the row
+    // advances by a constant when the engine's permutation is affine along that stride
+    const int D = blockDim.x >> lgRB, ps = E::pos_stride(D, fd), r0 = threadIdx.x & (RB - 1);
+    for (int t = 0; t < T_in; t++) {
+        xnl_input<T>(a, t, term, i);
+        V *R = Xb[t & 1], *Xn = Xb[(t + 1) & 1];
+        // S holds input t+1, completed inside the transform of input t: pre-process it
+        // beside the products of input t
+        if (t + 1 < T_in) {
+            xnl_input<T>(a, t + 1, tn, in_);
+            c2r_pre_rm<T>(g, S, SK, Xn, RB, lgRB, tn == 0);
+        }
+        int q = E::pos(threadIdx.x >> lgRB, fd) * RB + r0;
+        if (term < 2) {
+            for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x, q += ps * RB) {
+                if (ps < 0) q = E::pos(idx >> lgRB, fd) * RB + r0;
+                const V p = R[q];
+                if (term < 0) {
+                    U[i * H * RB + idx] = p;
+                } else if (term == 0) {
+                    const V u = U[idx];
+                    A[idx] = mk<T>(u.x * p.x, u.y * p.y);
+                } else {
+                    const V u = U[H * RB + idx];
+                    A[idx] = mk<T>(A[idx].x + u.x * p.x, A[idx].y + u.y * p.y);
+                }
+            }
+        } else {
+            // (acc + u_z d/dz v_i) * tmp in place
+            for (int idx = threadIdx.x; idx < H * RB; idx += blockDim.x, q += ps * RB) {
+                if (ps < 0) q = E::pos(idx >> lgRB, fd) * RB + r0;
+                const V u = U[2 * H * RB + idx], p = R[q], acc = A[idx];
+                R[q] = mk<T>((acc.x + u.x * p.x) * tmp, (acc.y + u.y * p.y) * tmp);
+            }
+        }
+        __syncthreads();  // S consumed, Xn pre-processed, the products of input t done
+        if (t + 2 < T_in) rows_load_rm(S, xnl_input<T>(a, t + 2, tn, in_) + off, ld, nxh, RB, nv, SK);
+        if (term == 2) {
+            // forward transform from permuted order; R2C post-processing into A (free until the
+            // next component's first product, which comes after the next transform's barriers)
+            E::run_perm(R, nullptr, RB, fd, -1);
+            r2c_post_rm<T, E>(g, fd, R, A, SK, RB, lgRB);
+            __syncthreads();
+            rows_store_rm((V *)a.out[i] + off, ld, A, SK, nxh, nv);
+        }
+        if (t + 1 < T_in) E::run_wait(Xn, nullptr, RB, fd, +1);
+    }
+}
+
 // shared memory of k_x_nonlinear: X, S, U[3][H], A[H] for RB rows
 template <class E>
 __host__ __device__ inline size_t x_nl_elems(const typename E::Desc &fd, int nxh, int H, int RB) {
@@ -627,7 +823,11 @@ __device__ __forceinline__ void x_nonlinear_body(const Geo &g, const typename E:
 }
 template <typename T, class E, int CRB = 0>
 __global__ void __launch_bounds__(kThreads, E::kMinBlocks) k_x_nonlinear(Geo g, typename E::Desc fd, XNLArgs a, int RBrt) {
-    x_nonlinear_body<T, E, CRB>(g, fd, a, RBrt, blockIdx);
+    if constexpr (E::kBuffers == 1 && CRB != 0 && sizeof(T) == 4) {
+        x_nonlinear_pipe<T, E, CRB>(g, fd, a);  // four-step engine, FP32, fixed row count
+    } else {
+        x_nonlinear_body<T, E, CRB>(g, fd, a, RBrt, blockIdx);
+    }
 }
 
 // ---------------------------------------------------------------------------------
