@@ -369,6 +369,40 @@ __device__ void vel_update(const Geo &g, const typename E::Desc &fd, const Fused
     __syncthreads();
 }
 
+// vel_update of a component without buoyancy with its inputs already in shared memory: Uc the
+// nonlinear spectrum (natural rows), X and X + tile the stage input vin and the step start cold;
+// the same operations in the same order, the filtered term formed in place and the updated
+// component left in X (as vel_update with to_x).  Each thread reads only the elements it writes.
+template <typename T>
+__device__ void vel_update_prefetched(const Geo &g, const FusedArgs &a, const ColTile &t, int c3, C2<T> *Uc, C2<T> *X) {
+    using V = C2<T>;
+    const int nz = g.nz, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
+    const int tile = nz * TK;
+    const T dt = pick<T>(a.dt, a.f_dt, a.q_dt), nu = pick<T>(a.nu, a.f_nu, a.q_nu), rmp = pick<T>(a.rmp, a.f_rmp, a.q_rmp);
+    const V *va = (const V *)a.vin[(c3 + 1) % 3], *vb = (const V *)a.vin[(c3 + 2) % 3];
+    const T oa = pick<T>(a.omega[(c3 + 1) % 3], a.f_omega[(c3 + 1) % 3], a.q_omega[(c3 + 1) % 3]);
+    const T ob = pick<T>(a.omega[(c3 + 2) % 3], a.f_omega[(c3 + 2) % 3], a.q_omega[(c3 + 2) % 3]);
+    for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+        const int k = idx >> lgTK, c = idx & (TK - 1);
+        if (c >= nv) { X[idx] = mk<T>(0, 0); continue; }
+        const int kx = kx0 + c;
+        V n = Uc[idx];
+        if (a.rot) {
+            const unsigned q = fidx<T>(g, k, ky, kx);
+            const V pa = va[q], pb = vb[q];
+            n = mk<T>(n.x + (T)2 * (oa * pb.x - ob * pa.x), n.y + (T)2 * (oa * pb.y - ob * pa.y));
+        }
+        n = cscale(n, g.FX<T>(kx));
+        n = cscale(n, g.FY<T>(ky));
+        n = cscale(n, g.FZ<T>(k));
+        const T k2 = g.KX<T>(kx) * g.KX<T>(kx) + g.KY<T>(ky) * g.KY<T>(ky) + g.KZ<T>(k) * g.KZ<T>(k);
+        const V v = X[idx], cv = X[tile + idx];
+        const V lap = cscale(v, -k2);
+        X[idx] = mk<T>(cv.x + dt * (nu * lap.x - n.x) * rmp, cv.y + dt * (nu * lap.y - n.y) * rmp);
+    }
+    __syncthreads();
+}
+
 // goto_domain_w_boundaries, noslip_z, goto_3d_fourier for component c3 in {0, 1}
 // (boundary_mod.fpp:72-194, vboundary.f90:154-211): z-inverse, 1/nz on the physical rows, wall
 // rows from the previous stage's pressure, continuation and z-forward; Uc in and out.
@@ -812,6 +846,22 @@ __device__ __forceinline__ void fused_vcomp_body(const Geo &g, const typename E:
     V *X = Uc + (size_t)nz * TK;
     V *Y = X + (size_t)fd.L * TK;
     const bool buoy = c3 == 2 && a.bouss;
+    V *w = (V *)a.work[c3];
+    if constexpr (E::kZoom) {
+        if (c3 < 2 && a.nl_spec && fd.ztab) {
+            // all three input tiles requested at once: vin and cold by asynchronous copies into
+            // the FFT buffer, the FP32 nonlinear spectrum by converting loads into Uc
+            const int tile = nz * TK;
+            tile_load_async(X, (const V *)a.vin[c3] + t.col0, t.zs, nz, TK, t.nv);
+            tile_load_async(X + tile, (const V *)a.cold[c3] + t.col0, t.zs, nz, TK, t.nv);
+            nl_tile_load<T>(Uc, a, c3, t.col0, t.zs, nz, TK, t.nv);
+            async_wait();
+            __syncthreads();
+            vel_update_prefetched<T>(g, a, t, c3, Uc, X);
+            vel_walls<T, E>(g, fd, a, t, c3, Uc, X, Y, true, w);
+            return;
+        }
+    }
     nl_tile_load<T>(X, a, c3, t.col0, t.zs, nl_rows(g, a), TK, t.nv);
     if (buoy) {
         tile_load_async(Uc, (const V *)a.vin[3] + t.col0, t.zs, nz, TK, t.nv);
@@ -819,7 +869,6 @@ __device__ __forceinline__ void fused_vcomp_body(const Geo &g, const typename E:
     } else {
         async_wait();
     }
-    V *w = (V *)a.work[c3];
     if (c3 < 2) {
         // the update stays in the FFT buffer and the wall round trip stores its result directly
         vel_update<T, E>(g, fd, a, t, c3, Uc, X, Y, buoy, true);

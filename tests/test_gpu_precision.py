@@ -172,6 +172,34 @@ def test_nl_fp32_channel():
     assert max(e) < 1e-5
 
 
+def test_state_conversions_round_trip():
+    """A precision-form solver call converts its FP64 state to float-float and back; with no
+    steps the state must come back to 2^-46 relative, zeros as zeros, and magnitudes below the
+    float range as (near) zero."""
+    from specter_gb300 import api
+    plan = api.Plan((16, 16, 58), (0, 0, 25), (0, 0, 5), (1.0, 1.0, 2.0), precision=api.FP64)
+    s = api.Solver(plan, api.BOUSS, fused=True, nl_fp32=True, dt=1e-5, nu=1e-4, kappa=1e-4)
+    rng = np.random.default_rng(31)
+    shape = plan.sshape
+    mag = 10.0 ** rng.uniform(-30, 30, shape)
+    a = (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) * mag
+    a.flat[::7] = 0.0
+    a.flat[3::11] *= 1e-280       # below the float range: the FP64 path
+    a.flat[5::13] = -a.flat[5::13]
+    fields = (s.vx, s.vy, s.vz, s.th, s.pr)
+    for f in fields:
+        f.upload(a)
+    s.step(0)
+    for f in fields:
+        b = f.download()
+        for x, y in ((a.real, b.real), (a.imag, b.imag)):
+            big = np.abs(x) >= 2.0 ** -100
+            assert np.all(np.abs(y[big] - x[big]) <= 2.0 ** -46 * np.abs(x[big]))
+            assert np.all(np.abs(y[~big]) <= 1e-30)
+            assert np.all(y[x == 0] == 0)
+    s.close()
+
+
 def test_nl_fp32_needs_fp64_plan():
     from specter_gb300 import api, SpecterError
     plan = api.Plan((16, 16, 58), (0, 0, 25), (0, 0, 5), (1.0, 1.0, 2.0), precision=api.FP32)
