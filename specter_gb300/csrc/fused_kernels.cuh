@@ -369,36 +369,59 @@ __device__ void vel_update(const Geo &g, const typename E::Desc &fd, const Fused
     __syncthreads();
 }
 
-// vel_update of a component without buoyancy with its inputs already in shared memory: Uc the
-// nonlinear spectrum (natural rows), X and X + tile the stage input vin and the step start cold;
-// the same operations in the same order, the filtered term formed in place and the updated
-// component left in X (as vel_update with to_x).  Each thread reads only the elements it writes.
+// The RK update of one component in the float-float kernels with window tables, without a staging
+// buffer: the stage input and the step start are in X and X + tile; the FP32 nonlinear spectrum
+// nl and the field ex of the linear coupling (theta for vz's buoyancy, vz for theta's heat
+// current; coefficient cx) are read from global memory, four elements per thread in flight:
+//   n = fc_filter(nl [+ 2 Om x v] - cx ex),  X = cold + dt (diff lap(X) - n) rmp,
+// the operations and their order those of vel_update and the scalar kernel.  rot_c3 >= 0 adds the
+// Coriolis term of that velocity component.
 template <typename T>
-__device__ void vel_update_prefetched(const Geo &g, const FusedArgs &a, const ColTile &t, int c3, C2<T> *Uc, C2<T> *X) {
+__device__ void update_direct(const Geo &g, const FusedArgs &a, const ColTile &t, C2<T> *X, const float2 *nl,
+                              const C2<T> *ex, T cx, T diff, int rot_c3) {
     using V = C2<T>;
+    constexpr int kB = 4;
     const int nz = g.nz, TK = t.TK, lgTK = t.lgTK, kx0 = t.kx0, ky = t.ky, nv = t.nv;
-    const int tile = nz * TK;
-    const T dt = pick<T>(a.dt, a.f_dt, a.q_dt), nu = pick<T>(a.nu, a.f_nu, a.q_nu), rmp = pick<T>(a.rmp, a.f_rmp, a.q_rmp);
-    const V *va = (const V *)a.vin[(c3 + 1) % 3], *vb = (const V *)a.vin[(c3 + 2) % 3];
-    const T oa = pick<T>(a.omega[(c3 + 1) % 3], a.f_omega[(c3 + 1) % 3], a.q_omega[(c3 + 1) % 3]);
-    const T ob = pick<T>(a.omega[(c3 + 2) % 3], a.f_omega[(c3 + 2) % 3], a.q_omega[(c3 + 2) % 3]);
-    for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
-        const int k = idx >> lgTK, c = idx & (TK - 1);
-        if (c >= nv) { X[idx] = mk<T>(0, 0); continue; }
-        const int kx = kx0 + c;
-        V n = Uc[idx];
-        if (a.rot) {
-            const unsigned q = fidx<T>(g, k, ky, kx);
-            const V pa = va[q], pb = vb[q];
-            n = mk<T>(n.x + (T)2 * (oa * pb.x - ob * pa.x), n.y + (T)2 * (oa * pb.y - ob * pa.y));
+    const int tile = nz * TK, total = nz * TK;
+    const T dt = pick<T>(a.dt, a.f_dt, a.q_dt), rmp = pick<T>(a.rmp, a.f_rmp, a.q_rmp);
+    const float2 *nlc = nl + t.col0;
+    const V *exc = ex ? ex + t.col0 : nullptr;
+    for (int base = threadIdx.x; base < total; base += kB * blockDim.x) {
+        float2 f[kB];
+        V e[kB];
+#pragma unroll
+        for (int u = 0; u < kB; u++) {
+            const int idx = base + u * blockDim.x;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
+            const bool in = idx < total && c < nv;
+            const unsigned q = (unsigned)k * t.zs + (unsigned)c;
+            f[u] = in ? __ldg(nlc + q) : make_float2(0.f, 0.f);
+            e[u] = (in && exc) ? exc[q] : mk<T>(0, 0);
         }
-        n = cscale(n, g.FX<T>(kx));
-        n = cscale(n, g.FY<T>(ky));
-        n = cscale(n, g.FZ<T>(k));
-        const T k2 = g.KX<T>(kx) * g.KX<T>(kx) + g.KY<T>(ky) * g.KY<T>(ky) + g.KZ<T>(k) * g.KZ<T>(k);
-        const V v = X[idx], cv = X[tile + idx];
-        const V lap = cscale(v, -k2);
-        X[idx] = mk<T>(cv.x + dt * (nu * lap.x - n.x) * rmp, cv.y + dt * (nu * lap.y - n.y) * rmp);
+#pragma unroll
+        for (int u = 0; u < kB; u++) {
+            const int idx = base + u * blockDim.x;
+            if (idx >= total) continue;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
+            if (c >= nv) { X[idx] = mk<T>(0, 0); continue; }
+            const int kx = kx0 + c;
+            V n = from_f2<T>(f[u]);
+            if (rot_c3 >= 0) {  // component rot_c3 of 2 Om x v = 2 (Om_a v_b - Om_b v_a), (c3, a, b) cyclic
+                const int ia = (rot_c3 + 1) % 3, ib = (rot_c3 + 2) % 3;
+                const T oa = pick<T>(a.omega[ia], a.f_omega[ia], a.q_omega[ia]), ob = pick<T>(a.omega[ib], a.f_omega[ib], a.q_omega[ib]);
+                const unsigned q = fidx<T>(g, k, ky, kx);
+                const V pa = ((const V *)a.vin[ia])[q], pb = ((const V *)a.vin[ib])[q];
+                n = mk<T>(n.x + (T)2 * (oa * pb.x - ob * pa.x), n.y + (T)2 * (oa * pb.y - ob * pa.y));
+            }
+            if (exc) n = mk<T>(n.x - cx * e[u].x, n.y - cx * e[u].y);
+            n = cscale(n, g.FX<T>(kx));
+            n = cscale(n, g.FY<T>(ky));
+            n = cscale(n, g.FZ<T>(k));
+            const T k2 = g.KX<T>(kx) * g.KX<T>(kx) + g.KY<T>(ky) * g.KY<T>(ky) + g.KZ<T>(k) * g.KZ<T>(k);
+            const V v = X[idx], cv = X[tile + idx];
+            const V lap = cscale(v, -k2);
+            X[idx] = mk<T>(cv.x + dt * (diff * lap.x - n.x) * rmp, cv.y + dt * (diff * lap.y - n.y) * rmp);
+        }
     }
     __syncthreads();
 }
@@ -848,17 +871,25 @@ __device__ __forceinline__ void fused_vcomp_body(const Geo &g, const typename E:
     const bool buoy = c3 == 2 && a.bouss;
     V *w = (V *)a.work[c3];
     if constexpr (E::kZoom) {
-        if (c3 < 2 && a.nl_spec && fd.ztab) {
-            // all three input tiles requested at once: vin and cold by asynchronous copies into
-            // the FFT buffer, the FP32 nonlinear spectrum by converting loads into Uc
+        if (a.nl_spec && fd.ztab) {
+            // no staging buffer (more L1 for the transform tables): vin and cold by asynchronous
+            // copies into the FFT buffer, the nonlinear spectrum and theta read in the update
+            V *Xz = (V *)smem_raw;
             const int tile = nz * TK;
-            tile_load_async(X, (const V *)a.vin[c3] + t.col0, t.zs, nz, TK, t.nv);
-            tile_load_async(X + tile, (const V *)a.cold[c3] + t.col0, t.zs, nz, TK, t.nv);
-            nl_tile_load<T>(Uc, a, c3, t.col0, t.zs, nz, TK, t.nv);
+            tile_load_async(Xz, (const V *)a.vin[c3] + t.col0, t.zs, nz, TK, t.nv);
+            tile_load_async(Xz + tile, (const V *)a.cold[c3] + t.col0, t.zs, nz, TK, t.nv);
             async_wait();
             __syncthreads();
-            vel_update_prefetched<T>(g, a, t, c3, Uc, X);
-            vel_walls<T, E>(g, fd, a, t, c3, Uc, X, Y, true, w);
+            update_direct<T>(g, a, t, Xz, (const float2 *)a.nl[c3], buoy ? (const V *)a.vin[3] : nullptr,
+                             pick<T>(a.xmom, a.f_xmom, a.q_xmom), pick<T>(a.nu, a.f_nu, a.q_nu), a.rot ? c3 : -1);
+            if (c3 < 2) {
+                vel_walls<T, E>(g, fd, a, t, c3, nullptr, Xz, nullptr, true, w);
+                return;
+            }
+            for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+                const int k = idx >> t.lgTK, c = idx & (TK - 1);
+                if (c < t.nv) w[fidx<T>(g, k, t.ky, t.kx0 + c)] = Xz[idx];
+            }
             return;
         }
     }
@@ -928,17 +959,29 @@ __global__ void __launch_bounds__(E::kColThreads, E::kMinBlocks) k_fused_theta(G
     using V = C2<T>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nz = g.nz, nzp = g.nzp, L = fd.L;
+    // float-float kernels with window tables: no staging buffer (the update reads the nonlinear
+    // spectrum and vz from global memory), the FFT buffer first
+    bool direct = false;
+    if constexpr (E::kZoom) direct = fd.ztab && a.nl_spec;
     V *Th = (V *)smem_raw;
-    V *X = Th + (size_t)nz * TK;
+    V *X = direct ? Th : Th + (size_t)nz * TK;
     V *Y = X + (size_t)L * TK;
     const int kx0 = blockIdx.x * TK, ky = blockIdx.y;
     const int nv = min(TK, g.nxh - kx0);
     auto colq = [&](int z, int c) { return fidx<T>(g, z, ky, kx0 + c); };
     const T dt = pick<T>(a.dt, a.f_dt, a.q_dt), kap = pick<T>(a.kappa, a.f_kappa, a.q_kappa), rmp = pick<T>(a.rmp, a.f_rmp, a.q_rmp);
     const T inz = (T)1 / (T)nz, xtemp = pick<T>(a.xtemp, a.f_xtemp, a.q_xtemp);
+    if (direct) {
+        const ColTile t = col_tile<T>(g, TK, blockIdx);
+        tile_load_async(X, (const V *)a.vin[3] + t.col0, t.zs, nz, TK, nv);
+        tile_load_async(X + (size_t)nz * TK, (const V *)a.cold[3] + t.col0, t.zs, nz, TK, nv);
+        async_wait();
+        __syncthreads();
+        update_direct<T>(g, a, t, X, (const float2 *)a.nl[3], (const V *)a.vin[2], xtemp, kap, -1);
+    }
     // 1. NL_theta forward, heat current, filter, laplak, update.  vz is copied into Th while
     //    NL_theta is transformed; theta and cold go into the FFT buffer afterwards.
-    {
+    if (!direct) {
         const int tile = nz * TK;
         const size_t zs = (size_t)g.ny * g.ldx, col0 = (size_t)ky * g.ldx + kx0;
         const bool stage2 = (size_t)E::kBuffers * L >= 2 * (size_t)nz;

@@ -25,7 +25,11 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
             return (3 * (size_t)P.nz + E::kBuffers * L) * tk * es + (2 * thr + (size_t)tk * 2) * 16 +
                    (size_t)tk * sizeof(LapCol<T>);
         }
-        if (which == kFusedTheta || which == kFusedVComp) return ((size_t)P.nz + E::kBuffers * L) * tk * es;
+        if (which == kFusedTheta || which == kFusedVComp) {
+            if constexpr (E::kZoom)  // update_direct: the FFT buffer only
+                if (fd.ztab && a.nl_spec) return E::kBuffers * L * tk * es;
+            return ((size_t)P.nz + E::kBuffers * L) * tk * es;
+        }
         return E::kBuffers * L * 2 * es;
     };
     int tk = 2;
