@@ -681,15 +681,23 @@ __device__ void vel_project_streamed(const Geo &g, const typename E::Desc &fd, c
         const T kx_ = g.KX<T>(kxc), ky_ = g.KY<T>(ky);
         WallSum<T> ws, wsd;
         if (threadIdx.x < kstep * TK) {
-#pragma unroll 2
+            // the components of two rows requested before either is used (the loop is bound by
+            // the latency of these loads)
+            V nA = mk<T>(0, 0), nB = mk<T>(0, 0), nC = mk<T>(0, 0);
+            if (c < nv && k0 < nz) {
+                const unsigned q = fidx<T>(g, k0, ky, kx0 + c);
+                nA = ldg_v(w0 + q);
+                nB = ldg_v(w1 + q);
+                nC = ldg_v(w2 + q);
+            }
             for (int k = k0; k < nz; k += kstep) {
                 const int idx = k * TK + c;
-                V A = mk<T>(0, 0), B = mk<T>(0, 0), Cc = mk<T>(0, 0);
-                if (c < nv) {
-                    const unsigned q = fidx<T>(g, k, ky, kx0 + c);
-                    A = w0[q];
-                    B = w1[q];
-                    Cc = w2[q];
+                V A = nA, B = nB, Cc = nC;
+                if (c < nv && k + kstep < nz) {
+                    const unsigned q = fidx<T>(g, k + kstep, ky, kx0 + c);
+                    nA = ldg_v(w0 + q);
+                    nB = ldg_v(w1 + q);
+                    nC = ldg_v(w2 + q);
                 }
                 const T kz_ = g.KZ<T>(k);
                 const T k2 = kx_ * kx_ + ky_ * ky_ + kz_ * kz_;
@@ -785,16 +793,31 @@ __device__ void vel_project_streamed(const Geo &g, const typename E::Desc &fd, c
         const V *E1 = (const V *)a.hspec[0], *E2 = (const V *)a.hspec[1];
         tile_load_async(X, E1 + t.col0, t.zs, nz, TK, nv);
         tile_load_async(X + tile, E2 + t.col0, t.zs, nz, TK, nv);
-        async_wait();
-        __syncthreads();
         V *o0 = (V *)a.vout[0], *o1 = (V *)a.vout[1], *o2 = (V *)a.vout[2];
         const T ky_ = g.KY<T>(ky);
+        // the components of the next element requested before this one is used (L2 hits: the
+        // Poisson pass read them moments before); the first while the spectra tiles arrive
+        auto comp = [&](int idx, V &A, V &B, V &Cc) {
+            const int k = idx >> lgTK, c = idx & (TK - 1);
+            A = B = Cc = mk<T>(0, 0);
+            if (idx < nz * TK && c < nv) {
+                const unsigned q = fidx<T>(g, k, ky, kx0 + c);
+                A = ldg_v(w0 + q);
+                B = ldg_v(w1 + q);
+                Cc = ldg_v(w2 + q);
+            }
+        };
+        V nA, nB, nC;
+        comp(threadIdx.x, nA, nB, nC);
+        async_wait();
+        __syncthreads();
         for (int idx = threadIdx.x; idx < nz * TK; idx += blockDim.x) {
+            V A = nA, B = nB, Cc = nC;
+            comp(idx + blockDim.x, nA, nB, nC);
             const int k = idx >> lgTK, c = idx & (TK - 1);
             if (c >= nv) continue;
             const int kx = kx0 + c;
             const unsigned q = fidx<T>(g, k, ky, kx);
-            V A = w0[q], B = w1[q], Cc = w2[q];
             const V D = Dsv[idx];
             const T kx_ = g.KX<T>(kx), kz_ = g.KZ<T>(k);
             A = csub(A, cimk(kx_, D));
