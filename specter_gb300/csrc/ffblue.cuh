@@ -28,8 +28,8 @@
 // 3 x 3 Cooley-Tukey form with four constant twiddles, DFT_8 two DFT_4 and the w_8 rotations.
 //
 // Tables (FFBTab, ffc units): twiddles, chirp and filter, 45.5 KB per length, read through the
-// read-only cache (TS = false) or from a copy in shared memory (TS = true).  Any n <= L/2 = 540
-// runs on the same split; the plans use it for 270 < n <= 540.
+// read-only cache (a copy staged in shared memory measured no faster).  Any n <= L/2 = 540 runs
+// on the same split; the plans use it for 270 < n <= 540.
 #pragma once
 
 #include "common.cuh"
@@ -225,19 +225,15 @@ __device__ __forceinline__ void dft15(Q (&a)[15]) {
     }
 }
 
-template <bool TS>
-__device__ __forceinline__ Q tab_ld(const Q *p) {
-    if constexpr (TS) return *p;
-    else return ldg_v(p);
-}
+__device__ __forceinline__ Q tab_ld(const Q *p) { return ldg_v(p); }
 
 constexpr int ct_log2(int b) { return b <= 1 ? 0 : 1 + ct_log2(b / 2); }
 
 // Bluestein transform of the n natural rows of X (TK columns, X[row * TK + col]); rows [n, L) are
 // scratch.  sign > 0: X_j = sum_k x_k exp(+2 pi i j k / n) (z-inverse); sign < 0: the forward
-// transform.  NT threads run the block's loops; TS: the table pointer is in shared memory.
+// transform.  NT threads run the block's loops; the tables are read through the read-only cache.
 // Barriers: one after each step; the caller syncs after filling X.
-template <int TK, int NT, bool TS>
+template <int TK, int NT>
 __device__ __forceinline__ void bluestein(Q *X, const Q *tab, int n, int sign) {
     using T = FFBTab;
     constexpr int lgTK = ct_log2(TK);
@@ -254,14 +250,14 @@ __device__ __forceinline__ void bluestein(Q *X, const Q *tab, int n, int sign) {
             if (row < n) {
                 Q x = X[row * TK + c];
                 if (fwd) x = qconj(x);
-                a[n1] = qmul(x, tab_ld<TS>(chirp + row));
+                a[n1] = qmul(x, tab_ld(chirp + row));
             } else {
                 a[n1] = qzero();
             }
         }
         dft8_hz<-1>(a);
 #pragma unroll
-        for (int k1 = 1; k1 < 8; k1++) a[k1] = qmul(a[k1], tab_ld<TS>(tw1 + n2 * T::kTw1S + k1));
+        for (int k1 = 1; k1 < 8; k1++) a[k1] = qmul(a[k1], tab_ld(tw1 + n2 * T::kTw1S + k1));
 #pragma unroll
         for (int k1 = 0; k1 < 8; k1++) X[(np + T::M * k1) * TK + c] = a[k1];
     }
@@ -277,7 +273,7 @@ __device__ __forceinline__ void bluestein(Q *X, const Q *tab, int n, int sign) {
         dft15<-1>(b);
         const Q *tw = tw2 + n3 * T::kTw2S + k1;
 #pragma unroll
-        for (int k2 = 0; k2 < 15; k2++) X[(base + T::L3 * k2) * TK + c] = qmul(b[k2], tab_ld<TS>(tw + T::L1 * k2));
+        for (int k2 = 0; k2 < 15; k2++) X[(base + T::L3 * k2) * TK + c] = qmul(b[k2], tab_ld(tw + T::L1 * k2));
     }
     __syncthreads();
     // step C: DFT_9 over n3, filter, inverse DFT_9, w_1080^(-m3 (k1 + 8 k2))
@@ -296,13 +292,13 @@ __device__ __forceinline__ void bluestein(Q *X, const Q *tab, int n, int sign) {
             dft9<-1>(d);
             if (pass == 0) {
 #pragma unroll
-                for (int k3 = 0; k3 < 9; k3++) d[k3] = qconj(qmul(d[k3], tab_ld<TS>(fl + k3)));
+                for (int k3 = 0; k3 < 9; k3++) d[k3] = qconj(qmul(d[k3], tab_ld(fl + k3)));
             }
         }
         const Q *tw = tw2 + k1 + T::L1 * k2;
         X[base * TK + c] = qconj(d[0]);
 #pragma unroll
-        for (int m3 = 1; m3 < 9; m3++) X[(base + m3) * TK + c] = qconj(qmul(d[m3], tab_ld<TS>(tw + m3 * T::kTw2S)));
+        for (int m3 = 1; m3 < 9; m3++) X[(base + m3) * TK + c] = qconj(qmul(d[m3], tab_ld(tw + m3 * T::kTw2S)));
     }
     __syncthreads();
     // step B': inverse DFT_15 over k2, w_120^(-m2 k1)
@@ -316,7 +312,7 @@ __device__ __forceinline__ void bluestein(Q *X, const Q *tab, int n, int sign) {
         dft15<+1>(b);
         X[base * TK + c] = b[0];
 #pragma unroll
-        for (int m2 = 1; m2 < 15; m2++) X[(base + T::L3 * m2) * TK + c] = qmulc(b[m2], tab_ld<TS>(tw1 + m2 * T::kTw1S + k1));
+        for (int m2 = 1; m2 < 15; m2++) X[(base + T::L3 * m2) * TK + c] = qmulc(b[m2], tab_ld(tw1 + m2 * T::kTw1S + k1));
     }
     __syncthreads();
     // step A': inverse DFT_8 over k1 -> m = m' + 135 m1 (natural), chirp; rows >= n are dropped
@@ -330,7 +326,7 @@ __device__ __forceinline__ void bluestein(Q *X, const Q *tab, int n, int sign) {
         for (int m1 = 0; m1 < 4; m1++) {
             const int row = mp + T::M * m1;
             if (row < n) {
-                Q o = qmul(a[m1], tab_ld<TS>(chirp + row));
+                Q o = qmul(a[m1], tab_ld(chirp + row));
                 if (fwd) o = qconj(o);
                 X[row * TK + c] = o;
             }
@@ -342,7 +338,7 @@ __device__ __forceinline__ void bluestein(Q *X, const Q *tab, int n, int sign) {
 // One out-of-line copy per tile width: the column kernels transform at several call sites.
 template <int TK, int NT>
 __device__ __noinline__ void run_out(Q *X, const Q *tab, int n, int sign) {
-    bluestein<TK, NT, false>(X, tab, n, sign);
+    bluestein<TK, NT>(X, tab, n, sign);
 }
 
 }  // namespace ffb
