@@ -77,14 +77,6 @@ __global__ void k_q2d(const ffc *src, double2 *dst, size_t n) {
         dst[q] = make_double2(ff_to_double(v.x), ff_to_double(v.y));
     }
 }
-// FP32 copy of a float-float field: the nonlinear term's input.  The pairs may be unnormalised
-// (ff.cuh), so the copy is the rounded sum of both words, not the leading word.
-__global__ void k_q2f(const ffc *src, float2 *dst, size_t n) {
-    for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
-        const float4 v = *(const float4 *)(src + q);
-        dst[q] = make_float2(v.x + v.y, v.z + v.w);
-    }
-}
 
 static int convert(Plan &P, const void *src, void *dst, bool to_ff, const char *what) {
     const size_t n = P.field_elems();
@@ -291,19 +283,27 @@ static int run_stage(Plan &P, FusedState *fs, int o, const void *const vin[4], c
         Plan &Q = *fs->nlp;
         for (int k = 0; k < 3; k++) Q.tile_cap[k] = P.tile_cap[k];  // the autotuned z, y, x caps
         const size_t n = P.field_elems();
-        for (int i = 0; i < fs->nc; i++) {
-            Launch L_(P, "narrow_state", 24.0 * n);
-            if constexpr (is_ff<T>) k_q2f<<<152 * 8, 256, 0, P.stream>>>((const ffc *)vin[i], (float2 *)fs->v32[i], n);
-            else k_narrow<<<152 * 8, 256, 0, P.stream>>>((const double2 *)vin[i], (float2 *)fs->v32[i], n);
+        // float-float state: the FP32 z-inverse of the nonlinear term reads it directly (the rounded
+        // sum of each pair); an FP64 state is narrowed into the FP32 copies first
+        const void *in32[4] = {fs->v32[0], fs->v32[1], fs->v32[2], fs->v32[3]};
+        if constexpr (is_ff<T>) {
+            Q.nl_input_ff = 1;
+            for (int i = 0; i < 4; i++) in32[i] = vin[i];
+        } else {
+            Q.nl_input_ff = 0;
+            for (int i = 0; i < fs->nc; i++) {
+                Launch L_(P, "narrow_state", 24.0 * n);
+                k_narrow<<<152 * 8, 256, 0, P.stream>>>((const double2 *)vin[i], (float2 *)fs->v32[i], n);
+            }
+            if ((st = check_launch("narrow_state"))) return st;
         }
-        if ((st = check_launch("narrow_state"))) return st;
-        const void *v3[3] = {fs->v32[0], fs->v32[1], fs->v32[2]};
+        const void *v3[3] = {in32[0], in32[1], in32[2]};
         // the FP32 pipeline finishes the nonlinear term with its forward z transform (with
         // continuation): the FP64 column kernels read spectra and transform only the state
         void *spec[4] = {nullptr, nullptr, nullptr, nullptr};
         for (int c = 0; c < fs->nc; c++)
             if (!(spec[c] = Q.scratch_field(16 + c))) { set_error("out of device memory (NL spectra)"); return ERR_OOM; }
-        st = Ops<float>::nonlinear(Q, v3, bouss ? fs->v32[3] : nullptr, spec, 0, bouss ? 4 : 3, nullptr);
+        st = Ops<float>::nonlinear(Q, v3, bouss ? in32[3] : nullptr, spec, 0, bouss ? 4 : 3, nullptr);
         for (int c = 0; c < 4; c++) nl[c] = spec[c];
     } else if constexpr (!is_ff<T>) {
         const void *v3[3] = {vin[0], vin[1], vin[2]};

@@ -150,9 +150,34 @@ struct ZInvArgs {
     int scale_rows;   // rows [0, scale_rows) scaled, the rest copied unscaled
     double scale;
     int staged;       // 1: the input tile is staged once in smem (some field has two outputs)
+    int in_ff;        // FP32 kernels: the inputs are float-float fields, read as the rounded sum of
+                      // each pair (the precision form's nonlinear term reads its state so)
     float scale_f;
     ZInvArgs prepared() const { ZInvArgs b = *this; b.scale_f = (float)scale; return b; }
 };
+
+// [rows][TK] tile of a float-float complex field as FP32 values (the rounded sum of each pair),
+// element (k, c) from src[k * stride + c] for c < nv, zero for nv <= c < TK; eight 16-byte loads
+// per thread in flight.  Visible to the block after the caller's barrier.
+__device__ __forceinline__ void tile_load_ff_as_f32(float2 *dst, const ffc *src, unsigned stride, int rows, int TK,
+                                                    int nv) {
+    const int lgTK = lg2(TK), total = rows * TK;
+    for (int base = threadIdx.x; base < total; base += 8 * blockDim.x) {
+        float4 f[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int idx = base + u * blockDim.x;
+            const int k = idx >> lgTK, c = idx & (TK - 1);
+            f[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (idx < total && c < nv) f[u] = __ldg((const float4 *)(src + ((unsigned)k * stride + (unsigned)c)));
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int idx = base + u * blockDim.x;
+            if (idx < total) dst[idx] = make_float2(f[u].x + f[u].y, f[u].z + f[u].w);
+        }
+    }
+}
 
 template <typename T, class E, int CTK>
 __device__ __forceinline__ void z_inverse_body(const Geo &g, const typename E::Desc &fd, const ZInvArgs &a, int TKrt, uint3 blockIdx) {
@@ -168,7 +193,17 @@ __device__ __forceinline__ void z_inverse_body(const Geo &g, const typename E::D
     const unsigned zstride = (unsigned)g.ny * g.ldx;
     const V *src = in + (unsigned)ky * g.ldx + kx0;
     const T sc = pick<T>(a.scale, a.scale_f);
-    if (a.staged) tile_load_async(S, src, zstride, g.nz, TK, nv);
+    // float-float inputs (FP32 kernels only): converting loads in place of the asynchronous copies
+    auto load_tile = [&](V *dst) {
+        if constexpr (is_f32<T>) {
+            if (a.in_ff) {
+                tile_load_ff_as_f32(dst, (const ffc *)a.in[f] + (unsigned)ky * g.ldx + kx0, zstride, g.nz, TK, nv);
+                return;
+            }
+        }
+        tile_load_async(dst, src, zstride, g.nz, TK, nv);
+    };
+    if (a.staged) load_tile(S);
     for (int pass = 1; pass >= 0; pass--) {  // derivative output first: out0 may alias in
         V *out = (V *)(pass == 0 ? a.out0[f] : a.out1[f]);
         if (!out) continue;
@@ -180,7 +215,7 @@ __device__ __forceinline__ void z_inverse_body(const Geo &g, const typename E::D
                 X[idx] = pass == 1 ? cimk(g.KZ<T>(idx >> lgTK), v) : v;
             }
         } else {
-            tile_load_async(X, src, zstride, g.nz, TK, nv);
+            load_tile(X);
             async_wait();
             if (pass == 1) {
                 __syncthreads();

@@ -303,6 +303,7 @@ int Ops<T>::nonlinear(Plan &P, const void *const v[3], const void *th, void *con
         nf++;
     }
     z.nrows = nzp; z.scale_rows = 0; z.scale = 1.0;
+    z.in_ff = P.nl_input_ff;
     SG_TRY(launch_z_inverse<T>(P, z, nf));
     // y inverse A: U_c = S[8+c], DY_c = S[12+c]
     YArgs y{};

@@ -127,6 +127,9 @@ struct Plan {
     // on that engine, wall round trips as window corrections of the spectrum (1) or as an inverse
     // and a forward transform (0)
     int ff_zoom = 1;
+    // FP32 companion plans of the precision form: the nonlinear term's inputs are the owner's
+    // float-float state fields (z_inverse reads the rounded sum of each pair)
+    int nl_input_ff = 0;
     int capped(int t, int kind) const { return t < tile_cap[kind] ? t : tile_cap[kind]; }
     long long launches = 0;
     bool profile = false;
