@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 ROOT = os.path.dirname(HERE)
 LIB = os.path.join(HERE, "libspecter_gpu.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["plan.cu", "ops_f64.cu", "ops_f32.cu", "fast_f32.cu", "fast_x_f32.cu", "fast_y_f32.cu", "fused.cu", "fused_ffb.cu", "fused_fast_f32.cu", "fused_small_f32.cu", "noalloc.cu", "capi.cu"]
+SOURCES = ["plan.cu", "ops_f64.cu", "ops_f32.cu", "fast_f32.cu", "fast_x_f32.cu", "fast_y_f32.cu", "fused.cu", "fused_ffb.cu", "fused_ffb_pair.cu", "fused_ff_generic.cu", "fused_fast_f32.cu", "fused_small_f32.cu", "noalloc.cu", "capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xcompiler", "-Wno-deprecated-declarations"]

@@ -262,8 +262,7 @@ static int launch(Plan &P, const FusedState *fs, const FusedArgs &a, int which, 
             }
             return ffb_fused(P, d, a, which, bytes);
         }
-        if (P.ff_threads == 256) return launch_fused<ff, GenericFFT<ff, 256>>(P, fs->tzq.d, a, which, bytes);
-        return launch_fused<ff, GenericFFT<ff, 384>>(P, fs->tzq.d, a, which, bytes);
+        return ff_generic_fused(P, fs->tzq.d, a, which, bytes);
     } else {
         const int st = fast_fused(P, a, which, bytes);
         if (st != kNoFast) return st;

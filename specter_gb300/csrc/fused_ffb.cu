@@ -157,7 +157,7 @@ int ffb_fused(Plan &P, const FFBDesc &d, const FusedArgs &a, int which, double b
     // the projection's FP32 pressure transform uses this translation unit's constant twiddles
     if (fft4_ensure_tables() != cudaSuccess) { set_error("constant table upload failed"); return ERR_CUDA; }
     const bool pair = which == kFusedVProj ? P.ff_pair_proj : P.ff_pair_cols;
-    if (pair) return launch_fused<ff, FFBlue<288, 2>, 4>(P, d, a, which, bytes);
+    if (pair) return ffb_fused_pair(P, d, a, which, bytes);
     return launch_fused<ff, FFBlue<576>, 8>(P, d, a, which, bytes);
 }
 

@@ -53,7 +53,9 @@ int launch_fused(Plan &P, const typename E::Desc &fd, const FusedArgs &a, int wh
                        : which == kFusedVComp  ? "fused_vcomp"
                        : which == kFusedVProj  ? "fused_vproj"
                                                : "theta_herm";
-    if (P.batch && (which == kFusedVComp || which == kFusedVProj)) {  // record (batch.h)
+    if constexpr (is_ff<T>) {  // float-float solvers are not batched (specter_batch_create)
+        if (P.batch) { set_error("float-float column kernels have no batched form"); return ERR_STATE; }
+    } else if (P.batch && (which == kFusedVComp || which == kFusedVProj)) {  // record (batch.h)
         using R = PassRec<E, FusedArgs>;
         const R r{{0, cdiv(P.nxh, tk), P.ny, which == kFusedVComp ? 3 : 1}, P.geo, fd, a.prepared(), tk};
         if (which == kFusedVComp)
@@ -108,7 +110,12 @@ struct FFBTable {
 // n = nz + C; window: first row j0 = nzp - d and win = C + 2d rows
 int build_ffb_table(FFBTable &t, int n, int j0, int win);
 void free_ffb_table(FFBTable &t);
-// the float-float column kernels on that engine (fused_ffb.cu)
+// the float-float column kernels on that engine: one 576-thread block per SM (fused_ffb.cu) or two
+// 288-thread blocks (fused_ffb_pair.cu)
 int ffb_fused(Plan &P, const FFBDesc &d, const FusedArgs &a, int which, double bytes);
+int ffb_fused_pair(Plan &P, const FFBDesc &d, const FusedArgs &a, int which, double bytes);
+// the float-float column kernels on the generic Stockham engine, P.ff_threads threads a block
+// (fused_ff_generic.cu)
+int ff_generic_fused(Plan &P, const FFTDesc &d, const FusedArgs &a, int which, double bytes);
 
 }  // namespace sg
